@@ -1,0 +1,394 @@
+"""Benchmark of the Steinbach multi-phase-field time step on GB300.
+
+Workload (default): the 3D FP32-compensated configuration -- 256^3 cells,
+200 Voronoi ferrite grains + 2000 austenite nuclei (radius 2 cells), up to 4
+active grains per cell, C 0.10 / Mn 1.5 wt% with +-0.02 wt% uniform noise,
+T = 1013 K.  One "step" is one full time step: the phase sweep plus n_sub
+diffusion sub-steps (n_sub = 10 at 1013 K).
+
+Printed JSON (rank 0, one line):
+  value    cell-updates/s of the FP32-compensated step with the state resident
+           in HBM, timed with CUDA events on the launching stream.
+  e2e      the same metric through the C ABI with host buffers: upload of the
+           reference-layout state from pinned memory, K x (step + statistics
+           read-back), download of the state, all inside the timed region.
+  roofline the diffusion sub-step kernel (the dominant one): algorithmic bytes
+           per launch / mean launch time (CUDA events around each launch).
+  fp64     the plain FP64 step (reference layout) on the same workload.
+  cpu_baseline  the FP64 CPU oracle on a bounded sample of the workload.
+
+--impl reference times the reference's CPU algorithm (the FP64 oracle, a
+restatement of the reference's OpenMP solver, which itself cannot be built here)
+on the host cores over the same workload, one bounded sample per step.
+
+Multi-GPU (--gpus N under torchrun): the path does not shard for one domain in
+this build, so each rank advances an independent replica (different seed);
+value = all ranks' cells x steps / max-over-ranks time ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "cell-updates/s & % HBM roofline: FP32 vs FP64 step; batch; adjoint/fwd ratio"
+UNIT = "cell-updates/s"
+
+
+def _peaks() -> dict:
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _workload(name: str):
+    from phasefield_gb300 import workloads as W
+
+    return W.WORKLOADS[name]
+
+
+def _model_for(wl, grid=None, tmp=None):
+    import phasefield_gb300 as pf
+    from phasefield_gb300 import workloads as W
+
+    d = tmp or tempfile.mkdtemp(prefix="pfbench_")
+    cfg = W.write_config(os.path.join(d, wl.name + ".txt"), grid=grid or wl.grid, dx=wl.dx, T=wl.T,
+                         num_grain=(wl.n_grains, 0, 0), num_nuclei=wl.n_nuclei, directory=d)
+    W.write_thermo(os.path.join(d, "thermo_steel.txt"))
+    return cfg, pf.read_model(cfg)
+
+
+def _scaled_spec(wl, grid):
+    """Spec for a sub-box of the workload keeping grain and nucleus densities."""
+    s = wl.spec()
+    frac = (grid[0] * grid[1] * grid[2]) / float(wl.N)
+    s.n_grains = max(2, int(round(wl.n_grains * frac)))
+    s.n_nuclei = int(round(wl.n_nuclei * frac))
+    s.n_particles = int(round(wl.n_particles * frac))
+    return s
+
+
+def cpu_sample(wl, threads: int | None = None):
+    """FP64 oracle on a bounded sample of the workload: returns (model, state, time, cells, label)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import phasefield_gb300 as pf
+    import pyoracle as po
+
+    gx, gy, gz = wl.grid
+    grid = (gx, gy, max(1, min(gz, 32))) if gz > 1 else (gx, gy, 1)
+    cfg, m = _model_for(wl, grid)
+    om = po.load_model(cfg)
+    st = pf.init_microstructure(m, _scaled_spec(wl, grid), 0.0)
+    if threads:
+        po.set_threads(threads)
+    label = (f"{grid[0]}x{grid[1]}x{grid[2]} periodic box of the {wl.name} workload (same grain/nucleus density), "
+             f"one FP64 step per sample")
+    return om, st, grid[0] * grid[1] * grid[2], label
+
+
+def run_reference(args) -> dict:
+    """--impl reference: the reference's CPU algorithm (FP64 oracle) on the host cores."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import build_oracle
+    import pyoracle as po
+
+    build_oracle.build_oracle()
+    wl = _workload(args.workload)
+    om, st, cells, label = cpu_sample(wl)
+    t = 0.0
+    for _ in range(args.warmup):
+        t = po.run(om, st, t, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t = po.run(om, st, t, 1)
+    dt = time.perf_counter() - t0
+    v = cells * args.steps / dt
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Voronoi grains + nuclei)",
+        "config": {"workload": wl.name, "sample": label},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": label},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
+    import numpy as np
+    import torch
+
+    import phasefield_gb300 as pf
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.cuda.current_device()
+    wl = _workload(args.workload)
+    cfg, m = _model_for(wl)
+    spec = wl.spec()
+    spec.seed = wl.seed + rank
+    st0 = pf.init_microstructure(m, spec, 0.0)
+    N = wl.N
+    P = pf.params_at(m, 0.0)
+    nsol = m.nsol
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- value: FP32-compensated step, state resident in HBM -------------
+    F = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    F.set_stream(stream.cuda_stream)
+    F.upload(st0, 0.0)
+    F.update(args.warmup)
+    F.enable_kernel_timing(True)
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        F.update(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    kt = F.kernel_times()
+    launches = kt["phase"][1] + kt["diffusion"][1]
+    value = world * N * args.steps / (ms / 1e3)
+    fr_end = F.fractions()
+    F.enable_kernel_timing(False)
+    F.close()
+
+    pk = _peaks()
+    diff_bytes = N * (12 + 16 * nsol)           # algorithmic bytes per diffusion sub-step
+    phase_bytes = N * (60 + 8 * nsol)           # algorithmic bytes per phase sweep
+    t_diff = kt["diffusion"][0] / max(1, kt["diffusion"][1]) / 1e3
+    t_phase = kt["phase"][0] / max(1, kt["phase"][1]) / 1e3
+    ach = diff_bytes / t_diff / 1e9
+    step_bytes = phase_bytes + P.n_sub * diff_bytes
+
+    # ---- FP64 plain step on the same workload ----------------------------
+    k64 = max(1, min(args.steps, args.fp64_steps))
+    G = pf.PhaseField(m, pf.PF_PREC_FP64)
+    G.set_stream(stream.cuda_stream)
+    G.upload(st0, 0.0)
+    G.update(1)
+    G.enable_kernel_timing(True)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    G.update(k64)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = max_over_ranks(g0.elapsed_time(g1))
+    kt64 = G.kernel_times()
+    G.close()
+    value64 = world * N * k64 / (ms64 / 1e3)
+
+    # ---- e2e: through the C ABI with pinned host buffers -----------------
+    keep_alive = []
+
+    def pinned(a: np.ndarray) -> np.ndarray:
+        t = torch.empty(a.size, dtype={np.int32: torch.int32, np.float64: torch.float64}[a.dtype.type],
+                        pin_memory=True)
+        keep_alive.append(t)
+        out = t.numpy()
+        out[:] = a
+        return out
+
+    host = {k: pinned(v) for k, v in st0.items()}
+    back = {k: pinned(np.zeros_like(v)) for k, v in st0.items()}
+    H = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    H.set_stream(stream.cuda_stream)
+    H.upload(host, 0.0)   # warm the path (allocations, module load)
+    H.update(1)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    H.upload(host, 0.0)
+    for _ in range(args.steps):
+        H.update(1)
+        H.fractions()  # device -> host read of the step's statistics (64 bytes)
+    import ctypes
+    L = pf.lib()
+    tt = ctypes.c_double()
+    pf.check(L.pf_download_state(H._ctx, pf._ptr(back["ids"]), pf._ptr(back["phi"]), pf._ptr(back["phase"]),
+                                 pf._ptr(back["conc"]), pf._ptr(back["C"]), ctypes.byref(tt)), "download")
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    H.close()
+    state_bytes = sum(int(v.nbytes) for k, v in st0.items() if k in ("ids", "phi", "phase", "C"))
+    down_bytes = sum(int(v.nbytes) for v in st0.values())
+    e2e = {"value": world * N * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(state_bytes / args.steps),
+           "d2h_bytes_per_step": int(64 + down_bytes / args.steps)}
+
+    if rank != 0:
+        return None
+
+    # ---- CPU baseline (oracle, bounded sample) ----------------------------
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import pyoracle as po
+
+        om, cst, cells, label = cpu_sample(wl)
+        tcur = po.run(om, cst, 0.0, 1)
+        c0 = time.perf_counter()
+        nst = 2
+        po.run(om, cst, tcur, nst)
+        cdt = time.perf_counter() - c0
+        cpu = {"value": cells * nst / cdt, "unit": UNIT, "cores": po.num_threads(), "kind": "port",
+               "sample": label + f", {nst} steps"}
+
+    ms_step = ms / args.steps
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 (Kahan-compensated solutes, fp64 reductions)",
+        "data": "synthetic (seeded Voronoi grains + nuclei, uniform noise)",
+        "config": {"workload": f"{wl.name}: {wl.grid[0]}x{wl.grid[1]}x{wl.grid[2]} cells, {wl.n_grains} grains, "
+                               f"{wl.n_nuclei} nuclei r={wl.nucleus_radius}, C/Mn {wl.C0} +-{wl.C_noise[0]} wt%, "
+                               f"T={wl.T} K, n_sub={P.n_sub}",
+                   "grid": list(wl.grid), "n_sub": P.n_sub, "solutes": nsol,
+                   "l2": f"inputs larger than L2 (FP32 state {N * 52 / 1e9:.2f} GB, L2 0.13 GB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / pk["hbm_gbs"], "traffic": None, "kernel": "k_diffuse_f32",
+                     "algorithmic_bytes_per_launch": diff_bytes, "mean_launch_ms": t_diff * 1e3,
+                     "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)"},
+        "kernels": {
+            "phase_sweep_f32": {"launches": kt["phase"][1], "mean_ms": t_phase * 1e3,
+                                "gbs": phase_bytes / t_phase / 1e9, "bytes_per_launch": phase_bytes},
+            "diffusion_f32": {"launches": kt["diffusion"][1], "mean_ms": t_diff * 1e3, "gbs": ach,
+                              "bytes_per_launch": diff_bytes},
+            "step_gbs_effective": step_bytes * args.steps / (ms / 1e3) / 1e9,
+        },
+        "fp64": {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
+                 "phase_ms": kt64["phase"][0] / max(1, kt64["phase"][1]),
+                 "diffusion_ms": kt64["diffusion"][0] / max(1, kt64["diffusion"][1])},
+        "fp32_over_fp64": value / value64,
+        "fractions_end": [float(x) for x in fr_end[:3]],
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="3d256")
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    import __graft_entry__
+
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if world > 1:
+        import torch
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        torch.distributed.barrier()
+        if rank != 0:
+            __graft_entry__.build()
+    out = run_ours(args, rank, world, local_rank)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * pfstep.h -- C ABI of libpfstep, the GB300 (sm_103a) Steinbach
+ * multi-phase-field time step.
+ *
+ * Two groups of entry points:
+ *
+ *  1. A drop-in for the reference's GPU plug-in, zhubq/PhaseField
+ *     C++-openmp-cuda/src/gpu_solver.h:18-23.  Same names, same argument
+ *     meaning, same return convention, so phase_field.cpp links against this
+ *     library unchanged.
+ *
+ *  2. A full-step API (pf_*) that keeps the whole state resident in HBM and
+ *     advances complete time steps (phase sweep + sub-cycled diffusion +
+ *     partitioning) on the GPU: phase_field::Update
+ *     (C++-openmp-cuda/src/phase_field.cpp:243-305) and its per-cell solvers
+ *     (solver.cpp:147-432).  Every pf_* call returns an int status (PF_OK = 0,
+ *     negative on error; pf_last_error() gives a message).  One context per
+ *     host thread; contexts share nothing.
+ *
+ * Layout at the boundary is the reference's (phase_field.h:81-89): Blitz
+ * fortranArray order with the slot / phase index fastest, then x, y, z.
+ *   ids   int32  [N*6]        grain ids (phase = id/100000, ids < 100000 are phase 1)
+ *   phi   double [N*6]        phase-field value of each slot
+ *   phase double [N*3]        phase fractions (ferrite, austenite, cementite)
+ *   conc  double [nsol][N*3]  solute concentration of each phase
+ *   C     double [nsol][N]    total solute concentration (solute 0 = carbon, 1 = Mn)
+ * with N = ix*iy*iz and cell n = i + ix*(j + iy*k).
+ */
+#ifndef PFSTEP_H
+#define PFSTEP_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* 1. Drop-in for gpu_solver.h                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces GPU_Init, gpu_solver.h:18 / gpu_solver.cpp:26-99.  Selects device 0
+ * and allocates the device buffers for an x*y*z grid.  Returns 1 when the GPU
+ * can be used, 0 when there is no device or not enough memory (the caller then
+ * falls back to its CPU solver, phase_field.cpp:364). */
+int GPU_Init(const int x, const int y, const int z);
+
+/* Replaces GPU_Diffusion_solver, gpu_solver.h:19 / gpu_solver.cpp:204-218.
+ * Copies the phase fractions and total carbon to the device, advances the
+ * multiphase diffusion over the interval dt in num_loop = ceil(dt/del_t)
+ * sub-steps with del_t = dx*dx/max(D)/dims*0.2f (dims = 3 if z > 1 else 2),
+ * each sub-step partitioning C into phase concentrations with
+ * c_i = (C - sum_j phase_j*c_ij)/(sum_j phase_j*k_ij) and applying the
+ * 6-neighbour flux sum_nb sum_p sqrt(phase_p^nb*phase_p)*(c_p^nb - c_p)*D_p,
+ * then copies C back into htotal_conc.  k and c are 3x3 column-major. */
+void GPU_Diffusion_solver(double *hdiffusivity, double *hpartition_k, double *hpartition_c,
+                          double *hvalue_phase, double *htotal_conc, int x, int y, int z, double dt,
+                          double dx);
+
+/* Replaces GPU_Cleanup, gpu_solver.h:23 / gpu_solver.cpp:223-239.  Frees the
+ * buffers of GPU_Init.  Unlike the reference it neither calls
+ * cudaDeviceReset (which would tear down every other user of the device in the
+ * process) nor exit(0) on a failed free. */
+void GPU_Cleanup(void);
+
+/* ------------------------------------------------------------------------ */
+/* 2. Full-step API                                                         */
+/* ------------------------------------------------------------------------ */
+
+#define PF_OK 0
+#define PF_ERR_ARG (-1)       /* invalid argument / state                   */
+#define PF_ERR_NOMEM (-2)     /* device or pinned-host allocation failed     */
+#define PF_ERR_CUDA (-3)      /* CUDA runtime error                          */
+#define PF_ERR_TIMEOUT (-4)   /* a bounded device-side wait ran out          */
+#define PF_ERR_NONFINITE (-5) /* NaN / Inf found in the state                */
+#define PF_ERR_IO (-6)        /* file missing / malformed                    */
+#define PF_ERR_NODEV (-7)     /* no CUDA device                              */
+#define PF_ERR_RANGE (-8)     /* value outside what the layout can hold      */
+
+#define PF_PREC_FP64 0   /* reference layout, FP64, bit-matching the CPU solver      */
+#define PF_PREC_FP32C 1  /* compact layout: 4 slots, uint16 ids, FP32 + Kahan solutes */
+
+#define PF_MAXT 64
+
+/* Parsed model: the configuration file (phase_field.cpp:166-330) and the
+ * thermodynamic file (thermo_functor.cpp:11-53).  3x3 tables are column-major
+ * with phase pair (i,j), 1-based, at (i-1)+3*(j-1). */
+typedef struct {
+    char directory[256];
+    int ix, iy, iz;
+    double dx;                 /* cell size, um */
+    int i_intf;                /* interface thickness in cells; eta = dx*i_intf */
+    double cutoff;
+    int num_grain[3];
+    double phase_fraction[3];
+    double init_conc[3];
+    int nT;                    /* temperature path: nT (time, T) points */
+    double T_time[PF_MAXT], T_temp[PF_MAXT];
+    double reduction;
+    int num_init_iteration;
+    double timestep_output;
+    int micro_out;
+    double num_nuclei;
+    double m0[9], mQ[9];       /* mobility prefactor (um^4/J/s) and activation energy (J/mol) */
+    double sigma[9];           /* interface energy, J/um^2 */
+    double D0[2][3], DQ[2][3]; /* solute diffusivity per phase: [0] carbon, [1] Mn */
+    char thermo_file[256];
+    int gpu_flag;
+    int nsol;                  /* 1 = carbon (reference); 2 when the Mn extension is present */
+    double mn_ratio[3];        /* Mn partition: c_Mn,p proportional to mn_ratio[p] */
+    double ent_a[9], ent_b[9];                 /* entropy k_ij = a*T + b */
+    double nple1_a[9], nple1_b[9], nple1_c[9]; /* parsed, unused by the step */
+    double nple2_a[9], nple2_b[9], nple2_c[9]; /* parsed, unused by the step */
+    double eq_a[9], eq_b[9], eq_c[9];          /* PARA equilibrium wt% = a*T^2 + b*T + c */
+} pf_model;
+
+/* Per-step parameters evaluated on the host (Update_parameter,
+ * phase_field.cpp:307-315; thermo_data::Get_data, thermo_data.cpp:24-41). */
+typedef struct {
+    int ix, iy, iz;
+    int nnb;            /* 2*dimensions */
+    int nsol;
+    int n_sub;          /* diffusion sub-steps per phase step */
+    long long N;
+    double T, time;
+    double dx, cutoff, eta;
+    double pfm_dt, diff_dt, dt_sub;
+    double factor1, factor2, factor3;
+    double coef_diff;
+    double m[9], sigma[9];
+    double entropy[9], eq[9], dcdT[9];
+    double D[2][3];
+    double k[2][9], c[2][9];
+} pf_step_params;
+
+/* Seeded synthetic microstructure (replaces the reference's unseeded
+ * Construct/Nucleate1in2, MicrostructureConstruction.cpp:4-65 and
+ * nucleation.cpp:3-43): periodic Voronoi ferrite grains (ids 100000+g),
+ * spherical austenite nuclei (ids 200000+n) and cementite particles
+ * (ids 300000+n) with tanh interfaces, uniform solutes plus uniform noise. */
+typedef struct {
+    uint64_t seed;
+    int n_grains;
+    int n_nuclei;
+    double nucleus_radius;    /* cells */
+    int n_particles;
+    double particle_radius;   /* cells */
+    double width;             /* interface width, cells */
+    double C0[2];             /* total solute, wt% */
+    double C_noise[2];        /* half-width of the uniform noise, wt% */
+    int max_slots;            /* slots filled per cell (<= 6) */
+} pf_init_spec;
+
+const char *pf_status_string(int status);
+const char *pf_last_error(void);
+/* sizeof(pf_model), sizeof(pf_step_params), sizeof(pf_init_spec): lets a
+ * binding check its struct mirrors against this build. */
+int pf_abi_sizes(long long out[3]);
+
+/* Parse the reference configuration file and the thermodynamic file it names
+ * (looked up relative to the working directory, then the config's directory). */
+int pf_model_read(const char *config_path, pf_model *out);
+int pf_thermo_read(const char *thermo_path, pf_model *out);
+/* Parameters of the step that starts at 'time'. */
+int pf_params_at(const pf_model *model, double time, pf_step_params *out);
+/* Fill host arrays (reference layout) with a seeded initial state at 'time'. */
+int pf_init_microstructure(const pf_model *model, const pf_init_spec *spec, double time, int32_t *ids,
+                           double *phi, double *phase, double *conc, double *C);
+
+typedef struct pf_ctx pf_ctx;
+int pf_create(const pf_model *model, int precision, pf_ctx **out);
+int pf_destroy(pf_ctx *ctx);
+/* Run on a caller-owned cudaStream_t (NULL = the context's own stream). */
+int pf_set_stream(pf_ctx *ctx, void *cuda_stream);
+int pf_upload_state(pf_ctx *ctx, const int32_t *ids, const double *phi, const double *phase,
+                    const double *conc, const double *C, double time);
+/* conc may be NULL. */
+int pf_download_state(pf_ctx *ctx, int32_t *ids, double *phi, double *phase, double *conc, double *C,
+                      double *time);
+/* Advance nsteps full time steps (asynchronous on the context's stream). */
+int pf_step(pf_ctx *ctx, int nsteps);
+/* FP64 statistics: out[0..2] sum of phase fractions over cells, out[3] sum of
+ * phi over slots with grain id < 100000, out[4..5] solute totals, out[6] 0,
+ * out[7] count of non-finite values.  Divide by N for write_data.cpp:14-18. */
+int pf_reduce(pf_ctx *ctx, double out[8]);
+int pf_synchronize(pf_ctx *ctx);
+int pf_get_time(pf_ctx *ctx, double *time);
+int pf_last_params(pf_ctx *ctx, pf_step_params *out);
+/* Number of cells whose upload kept only the 4 largest of >4 slots (FP32C). */
+int pf_truncated_cells(pf_ctx *ctx, long long *out);
+/* Bracket every kernel launch with CUDA events; read back accumulated times. */
+int pf_enable_kernel_timing(pf_ctx *ctx, int on);
+/* times[0]/counts[0]: phase sweep, [1]: diffusion sub-step. Synchronises. */
+int pf_kernel_times(pf_ctx *ctx, double times_ms[2], long long counts[2]);
+/* Capture steps with constant parameters in a CUDA graph and replay it. */
+int pf_use_graph(pf_ctx *ctx, int on);
+/* Reference output writers (write_data.cpp:3-82).  pf_write_data appends a
+ * fraction_time.txt row under 'directory' when the reference would (or when
+ * forced) and, if the model's micro_out flag is set, writes a VTI file. */
+int pf_write_data(pf_ctx *ctx, const char *directory, int forced, int *written);
+int pf_write_vti(const char *path, int ix, int iy, int iz, double dx, const int32_t *ids,
+                 const double *C);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

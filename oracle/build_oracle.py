@@ -1,0 +1,78 @@
+"""Build recipes for the checker side (test infrastructure only).
+
+* ``build_oracle()`` compiles the FP64 CPU oracle ``pf_oracle.c`` into
+  ``oracle/_build/liboracle.so`` with ``-ffp-contract=off`` (no fused
+  multiply-add, so its rounding matches the product's FP64 GPU path and the
+  reference's host arithmetic) and OpenMP.
+* ``build_ref()`` compiles the reference's own CUDA diffusion plug-in,
+  ``C++-openmp-cuda/src/gpu_solver.cpp`` from the read-only reference checkout,
+  into device-only cubins under ``oracle/_ref/`` (one with the default
+  multiply-add contraction, one with ``-fmad=false``).  Its two kernels,
+  ``GPU_Partitioning`` and ``Diff3D``, then run on the GPU as an independent
+  check of the oracle's partition and diffusion sub-step.  The host part of that
+  file and the rest of the reference (which needs Blitz++) are not built.  This
+  step only runs where the reference checkout exists; the cubins travel with
+  the repository copy.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(BUILD, "liboracle.so")
+REF_SRC = "/root/reference/C++-openmp-cuda/src"
+REF_CUBIN = os.path.join(REF_OUT, "gpu_solver_ref.cubin")
+REF_CUBIN_NOFMA = os.path.join(REF_OUT, "gpu_solver_ref_nofma.cubin")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build_oracle(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = [os.path.join(HERE, "pf_oracle.c"), os.path.join(HERE, "pf_oracle.h")]
+    if force or _newer(LIB, src + [__file__]):
+        cmd = ["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               "-fno-fast-math", src[0], "-o", LIB, "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+    return LIB
+
+
+def build_ref(force: bool = False) -> list[str]:
+    """Compile the reference's GPU plug-in kernels (where the checkout exists)."""
+    src = os.path.join(REF_SRC, "gpu_solver.cpp")
+    if not os.path.exists(src):
+        return [p for p in (REF_CUBIN, REF_CUBIN_NOFMA) if os.path.exists(p)]
+    os.makedirs(REF_OUT, exist_ok=True)
+    nvcc = os.path.join(CUDA_HOME, "bin", "nvcc")
+    if not os.path.exists(nvcc):
+        nvcc = shutil.which("nvcc") or "nvcc"
+    out = []
+    for target, extra in ((REF_CUBIN, []), (REF_CUBIN_NOFMA, ["-fmad=false"])):
+        if force or _newer(target, [src, __file__]):
+            # cudaDeviceProp::deviceOverlap (read by the host-only GPU_Init
+            # printout) no longer exists in CUDA 13; the macro maps it onto a
+            # member that does.  Device code is unaffected.
+            cmd = [nvcc, "-cubin", "-x", "cu", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                   "-DdeviceOverlap=asyncEngineCount", "-I", REF_SRC] + extra + [src, "-o", target]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("reference kernel build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+        out.append(target)
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle())
+    print(build_ref())

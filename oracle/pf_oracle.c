@@ -1,0 +1,405 @@
+/*
+ * pf_oracle.c -- FP64 CPU oracle of the Steinbach multi-phase-field step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker; never linked into the product).
+ * Parity unpinned for the phase sweep: the reference has no tests or golden
+ * outputs and cannot be built here (Blitz++ missing).  Every function cites
+ * the reference file:line (paths inside zhubq/PhaseField) it restates.  The
+ * arithmetic follows the reference's evaluation order operation by operation;
+ * build with -ffp-contract=off so that no multiply-add is fused.
+ */
+#include "pf_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static const double PFO_PI = 3.1415926; /* constant.h:7 (truncated on purpose) */
+static const double PFO_R = 8.314;      /* constant.h:8 */
+#define MAXGRAIN_PER_PHASE 100000       /* phase_field.h:19 */
+
+#define M3(a, i, j) ((a)[((i)-1) + 3 * ((j)-1)]) /* 1-based column-major 3x3 */
+
+int pfo_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void pfo_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* phase_field.h:25-29 */
+int pfo_phase_of_grain(int grain) {
+    if (grain == 0) return 0;
+    return (grain / MAXGRAIN_PER_PHASE > 0 ? grain / MAXGRAIN_PER_PHASE : 1);
+}
+
+/* phase_field.h:58-68 (Get_neighbor), restated 0-based */
+static inline int nb(int i, int len, int d) {
+    int g = i + d;
+    if (g >= len) g -= len;
+    else if (g < 0) g += len;
+    return g;
+}
+
+/* phase_field.cpp:232-242.  The reference leaves Temp uninitialised when no
+ * segment matches; the oracle returns the last profile temperature then. */
+double pfo_temperature(const pfo_model *m, double t) {
+    double Temp = m->T_temp[m->nT - 1];
+    for (int i = 0; i < m->nT - 1; i++)
+        if (t >= m->T_time[i] && t < m->T_time[i + 1])
+            Temp = (m->T_temp[i + 1] - m->T_temp[i]) / (m->T_time[i + 1] - m->T_time[i]) *
+                       (t - m->T_time[i]) + m->T_temp[i];
+    return Temp;
+}
+
+static double model_dims(const pfo_model *m) {
+    /* phase_field.cpp:354-362 */
+    double d = 3;
+    if (m->iz == 1) d -= 1;
+    if (m->iy == 1) d -= 1;
+    return d;
+}
+
+/* phase_field.cpp:307-315 (Update_parameter, without the time increment),
+ * thermo_data.cpp:24-41 (Get_data), phase_field.cpp:247-248 (sub-cycling). */
+void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
+    memset(p, 0, sizeof(*p));
+    const double T = pfo_temperature(m, time);
+    p->T = T;
+    p->dims = model_dims(m);
+    p->eta = m->dx * m->i_intf; /* phase_field.cpp:363 */
+    const double RT = PFO_R * T;
+    double maxms = -INFINITY;
+    for (int e = 0; e < 9; e++) {
+        p->m[e] = m->m0[e] * exp(-m->mQ[e] / RT);
+        double ms = p->m[e] * m->sigma[e];
+        if (ms > maxms) maxms = ms;
+    }
+    double maxD = -INFINITY;
+    for (int q = 0; q < m->nsol; q++)
+        for (int ph = 0; ph < 3; ph++) {
+            p->D[q][ph] = m->D0[q][ph] * exp(-m->DQ[q][ph] / RT);
+            if (p->D[q][ph] > maxD) maxD = p->D[q][ph];
+        }
+    p->pfm_dt = m->dx * m->dx / p->dims * 0.2 / maxms;
+    p->diff_dt = m->dx * m->dx / maxD / p->dims * 0.2;
+
+    /* thermo_data.cpp:25-32: functor evaluation; linear_functor.h:11-13,
+     * quadratic_functor.h:12-14.  Unset functors are zero. */
+    for (int j = 1; j <= 3; j++)
+        for (int i = 1; i <= 3; i++) {
+            const double x = T;
+            M3(p->entropy, i, j) = M3(m->ent_a, i, j) * x + M3(m->ent_b, i, j);
+            M3(p->eq, i, j) = M3(m->eq_a, i, j) * x * x + M3(m->eq_b, i, j) * x + M3(m->eq_c, i, j);
+            M3(p->dcdT, i, j) = (2 * M3(m->eq_a, i, j)) * x + M3(m->eq_b, i, j);
+        }
+    /* thermo_data.cpp:34-40 */
+    for (int i = 1; i <= 3; i++)
+        for (int j = 1; j <= 3; j++) {
+            if (i == j) M3(p->dcdT, i, j) = 1.;
+            M3(p->k[0], i, j) = M3(p->dcdT, j, i) / M3(p->dcdT, i, j);
+            M3(p->c[0], i, j) = M3(p->eq, j, i) - M3(p->k[0], i, j) * M3(p->eq, i, j);
+        }
+    /* Mn (no reference counterpart): linear partition c_i = (r_i/r_j) c_j. */
+    if (m->nsol > 1)
+        for (int i = 1; i <= 3; i++)
+            for (int j = 1; j <= 3; j++) {
+                M3(p->k[1], i, j) = m->mn_ratio[i - 1] / m->mn_ratio[j - 1];
+                M3(p->c[1], i, j) = 0.;
+            }
+    /* phase_field.cpp:247-248 */
+    int n = (int)ceil(p->pfm_dt / p->diff_dt);
+    p->n_sub = n > 1 ? n : 1;
+    p->dt_sub = p->pfm_dt / p->n_sub;
+}
+
+/* solver.cpp:389-405 */
+void pfo_partition(double C, const double *phase3, const double *k9, const double *c9, double *out3) {
+    for (int i = 1; i <= 3; i++) {
+        double t1 = 0., t2 = 0.;
+        for (int j = 1; j <= 3; j++) {
+            t1 += phase3[j - 1] * M3(k9, i, j);
+            t2 += phase3[j - 1] * M3(c9, i, j);
+        }
+        out3[i - 1] = (C - t2) / t1;
+    }
+}
+
+void pfo_partition_all(const pfo_model *m, const pfo_params *p, const double *phase,
+                       const double *C, double *conc) {
+    const long N = (long)m->ix * m->iy * m->iz;
+    for (int q = 0; q < m->nsol; q++) {
+#pragma omp parallel for schedule(static)
+        for (long n = 0; n < N; n++)
+            pfo_partition(C[q * N + n], phase + 3 * n, p->k[q], p->c[q], conc + q * 3 * N + 3 * n);
+    }
+}
+
+/* solver.cpp:374-387 (Driving_force); uses only the carbon concentration of phase ii */
+static inline double driving_force(const pfo_params *p, int phii, int phjj, double concii) {
+    double df = 0.;
+    if (phii != phjj)
+        df += M3(p->entropy, phii, phjj) * (concii - M3(p->eq, phii, phjj)) / M3(p->dcdT, phii, phjj);
+    return df;
+}
+
+/* solver.cpp:147-304 (Phase_field_solver) for cell (i,j,k), 0-based. */
+static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, int k,
+                       const int32_t *ids1, const double *phi1, int32_t *ids2, double *phi2,
+                       double *phase, double *conc1, const double *C) {
+    const int ix = m->ix, iy = m->iy, iz = m->iz;
+    const long N = (long)ix * iy * iz;
+    const long n = i + (long)ix * (j + (long)iy * k);
+    const double cutoff = m->cutoff;
+    /* solver.cpp:149-157: 1-based arrays of length 10, zero-initialised */
+    int sid[PFO_NSTENCIL + 1] = {0}, sph[PFO_NSTENCIL + 1] = {0};
+    double sv1[PFO_NSTENCIL + 1] = {0}, sv2[PFO_NSTENCIL + 1] = {0};
+    int num_local = 0, num = 0;
+    /* solver.cpp:159-166: neighbour order x-, x+, y-, y+, z-, z+ */
+    long nbr[6];
+    nbr[0] = nb(i, ix, -1) + (long)ix * (j + (long)iy * k);
+    nbr[1] = nb(i, ix, 1) + (long)ix * (j + (long)iy * k);
+    nbr[2] = i + (long)ix * (nb(j, iy, -1) + (long)iy * k);
+    nbr[3] = i + (long)ix * (nb(j, iy, 1) + (long)iy * k);
+    nbr[4] = i + (long)ix * (j + (long)iy * nb(k, iz, -1));
+    nbr[5] = i + (long)ix * (j + (long)iy * nb(k, iz, 1));
+
+    /* solver.cpp:168-175: own slots above cutoff, stored at their slot position */
+    for (int ii = 1; ii <= PFO_NSLOT; ii++) {
+        if (phi1[6 * n + ii - 1] > cutoff) {
+            num_local += 1;
+            sid[ii] = ids1[6 * n + ii - 1];
+            sph[ii] = pfo_phase_of_grain(ids1[6 * n + ii - 1]);
+            sv1[ii] = phi1[6 * n + ii - 1];
+        }
+    }
+    num = num_local;
+    /* solver.cpp:179-205: merge the neighbours' lists (break at id 0) */
+    for (int ii = 1; ii <= 2 * p->dims; ii++) {
+        const long q = nbr[ii - 1];
+        for (int jj = 1; jj <= PFO_NSLOT; jj++) {
+            int tid = ids1[6 * q + jj - 1];
+            if (tid == 0) break;
+            double tv = phi1[6 * q + jj - 1];
+            int kk;
+            for (kk = 1; kk <= PFO_NSTENCIL; kk++) {
+                if (tid == sid[kk]) {
+                    sv2[kk] += tv;
+                    break;
+                }
+            }
+            if (kk > PFO_NSTENCIL && num < PFO_NSTENCIL) {
+                num += 1;
+                sid[num] = tid;
+                sph[num] = pfo_phase_of_grain(tid);
+                sv2[num] += tv;
+            }
+        }
+    }
+    /* solver.cpp:207-216: bulk fast path */
+    if (num == 1) {
+        for (int ii = 0; ii < PFO_NSLOT; ii++) {
+            ids2[6 * n + ii] = ids1[6 * n + ii];
+            phi2[6 * n + ii] = phi1[6 * n + ii];
+        }
+        return;
+    }
+    /* solver.cpp:224-266 */
+    double del[PFO_NSTENCIL + 1] = {0};
+    const double factor1 = 1. / (m->dx * m->dx);
+    const double factor2 = PFO_PI * PFO_PI / (2. * p->eta * p->eta);
+    const double factor3 = PFO_PI / p->eta;
+    double local_conc[4];
+    for (int ii = 1; ii <= 3; ii++) local_conc[ii] = conc1[3 * n + ii - 1]; /* carbon */
+    for (int ii = 1; ii <= num; ii++) {
+        const int gi = sid[ii], phi_ = sph[ii];
+        (void)gi;
+        for (int jj = 1; jj <= num; jj++) {
+            if (ii == jj) continue;
+            const int phj = sph[jj];
+            if (abs(phi_ - phj) == 2) continue;
+            double d = 0.;
+            d = (sv2[ii] * sv1[jj] - sv2[jj] * sv1[ii]) * factor1;
+            d += (sv1[ii] - sv1[jj]) * factor2;
+            d *= M3(m->sigma, phi_, phj);
+            d += factor3 * sqrt(sv1[ii] * sv1[jj]) *
+                 driving_force(p, phi_, phj, local_conc[phi_]);
+            d *= M3(p->m, phi_, phj);
+            del[ii] += d;
+        }
+        del[ii] *= p->pfm_dt;
+        del[ii] += sv1[ii];
+        if (del[ii] > 1.0) del[ii] = 1.0;
+        else if (del[ii] < cutoff) del[ii] = 0.;
+    }
+    /* solver.cpp:270-271 */
+    for (int ii = 0; ii < 3; ii++) phase[3 * n + ii] = 0.;
+    /* solver.cpp:273 + 426-432: selection sort, first maximum wins */
+    for (int a = 1; a <= PFO_NSTENCIL; a++) {
+        int mx = a;
+        for (int b = a + 1; b <= PFO_NSTENCIL; b++)
+            if (del[b] > del[mx]) mx = b;
+        double tv = del[a]; del[a] = del[mx]; del[mx] = tv;
+        int ti = sid[a]; sid[a] = sid[mx]; sid[mx] = ti;
+    }
+    /* solver.cpp:276-296 */
+    double sum = 0.;
+    for (int ii = 1; ii <= PFO_NSLOT; ii++) {
+        if (del[ii] > cutoff) {
+            ids2[6 * n + ii - 1] = sid[ii];
+            phi2[6 * n + ii - 1] = del[ii];
+            int ph = pfo_phase_of_grain(sid[ii]);
+            phase[3 * n + ph - 1] += del[ii];
+            sum += del[ii];
+        } else {
+            ids2[6 * n + ii - 1] = 0;
+            phi2[6 * n + ii - 1] = 0.;
+        }
+    }
+    for (int ii = 0; ii < PFO_NSLOT; ii++) phi2[6 * n + ii] *= 1. / sum;
+    for (int ii = 0; ii < 3; ii++) phase[3 * n + ii] *= 1. / sum;
+    /* solver.cpp:299: partition in place (every solute) */
+    for (int q = 0; q < m->nsol; q++)
+        pfo_partition(C[q * N + n], phase + 3 * n, p->k[q], p->c[q], conc1 + q * 3 * N + 3 * n);
+}
+
+void pfo_phase_sweep(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phi1,
+                     int32_t *ids2, double *phi2, double *phase, double *conc1, const double *C) {
+    /* phase_field.cpp:252-257 */
+#pragma omp parallel for schedule(guided, 1) collapse(2)
+    for (int k = 0; k < m->iz; k++)
+        for (int j = 0; j < m->iy; j++)
+            for (int i = 0; i < m->ix; i++)
+                phase_cell(m, p, i, j, k, ids1, phi1, ids2, phi2, phase, conc1, C);
+}
+
+/* solver.cpp:343-372 (Diffusion_solver) for every solute */
+void pfo_diffusion_substep(const pfo_model *m, const pfo_params *p, double dt_sub, const double *phase,
+                           const double *conc1, double *conc2, double *C) {
+    const int ix = m->ix, iy = m->iy, iz = m->iz;
+    const long N = (long)ix * iy * iz;
+    const int nnb = (int)(2 * p->dims);
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < iz; k++)
+        for (int j = 0; j < iy; j++)
+            for (int i = 0; i < ix; i++) {
+                const long n = i + (long)ix * (j + (long)iy * k);
+                long nbr[6];
+                nbr[0] = nb(i, ix, -1) + (long)ix * (j + (long)iy * k);
+                nbr[1] = nb(i, ix, 1) + (long)ix * (j + (long)iy * k);
+                nbr[2] = i + (long)ix * (nb(j, iy, -1) + (long)iy * k);
+                nbr[3] = i + (long)ix * (nb(j, iy, 1) + (long)iy * k);
+                nbr[4] = i + (long)ix * (j + (long)iy * nb(k, iz, -1));
+                nbr[5] = i + (long)ix * (j + (long)iy * nb(k, iz, 1));
+                for (int q = 0; q < m->nsol; q++) {
+                    const double *c1 = conc1 + q * 3 * N;
+                    double del = 0.;
+                    for (int ii = 0; ii < nnb; ii++)
+                        for (int jj = 0; jj < 3; jj++)
+                            del += sqrt(phase[3 * nbr[ii] + jj] * phase[3 * n + jj]) *
+                                   (c1[3 * nbr[ii] + jj] - c1[3 * n + jj]) * p->D[q][jj];
+                    del *= (dt_sub / (m->dx * m->dx));
+                    C[q * N + n] += del;
+                    pfo_partition(C[q * N + n], phase + 3 * n, p->k[q], p->c[q],
+                                  conc2 + q * 3 * N + 3 * n);
+                }
+            }
+}
+
+/* phase_field.cpp:243-305, Update(false) on the CPU branch (GPU_Flag == 0). */
+void pfo_run(const pfo_model *m, pfo_state *s, double *time, int nsteps) {
+    const long N = (long)m->ix * m->iy * m->iz;
+    int32_t *ids_a = s->ids1, *ids_b = s->ids2;
+    double *phi_a = s->phi1, *phi_b = s->phi2;
+    double *conc_a = s->conc1, *conc_b = s->conc2;
+    for (int st = 0; st < nsteps; st++) {
+        pfo_params p;
+        pfo_params_at(m, *time, &p);
+        *time += p.pfm_dt; /* phase_field.cpp:314 */
+        pfo_phase_sweep(m, &p, ids_a, phi_a, ids_b, phi_b, s->phase, conc_a, s->C);
+        { int32_t *t = ids_a; ids_a = ids_b; ids_b = t; }
+        { double *t = phi_a; phi_a = phi_b; phi_b = t; }
+        for (int it = 1; it <= p.n_sub; it++) {
+            pfo_diffusion_substep(m, &p, p.dt_sub, s->phase, conc_a, conc_b, s->C);
+            double *t = conc_a; conc_a = conc_b; conc_b = t;
+        }
+    }
+    if (ids_a != s->ids1) {
+        memcpy(s->ids1, ids_a, sizeof(int32_t) * 6 * N);
+        memcpy(s->phi1, phi_a, sizeof(double) * 6 * N);
+        memcpy(s->ids2, ids_b, sizeof(int32_t) * 6 * N);
+        memcpy(s->phi2, phi_b, sizeof(double) * 6 * N);
+    }
+    if (conc_a != s->conc1) {
+        memcpy(s->conc1, conc_a, sizeof(double) * 3 * N * m->nsol);
+        memcpy(s->conc2, conc_b, sizeof(double) * 3 * N * m->nsol);
+    }
+}
+
+/* gpu_solver.cpp:204-218 with GPU_Partitioning (:131-154) and Diff3D (:160-188). */
+int pfo_gpu_diffusion_solver(const double *D3, const double *k9, const double *c9,
+                             const double *phase, double *C, int x, int y, int z,
+                             double dt, double dx, double *conc_out) {
+    const long N = (long)x * y * z;
+    int dims = (z > 1) ? 3 : 2; /* gpu_solver.cpp:93-94 */
+    double max_diff = D3[0];
+    for (int p = 1; p < 3; p++)
+        if (D3[p] > max_diff) max_diff = D3[p];
+    double del_t = dx * dx / max_diff / dims * 0.2f; /* 0.2f as in gpu_solver.cpp:207 */
+    int num_loop = (int)ceil(dt / del_t);
+    double dt_dxdx = dt / num_loop / (dx * dx);
+    double *conc = (double *)malloc(sizeof(double) * 3 * N);
+    if (!conc) return -1;
+    for (int it = 1; it <= num_loop; it++) {
+#pragma omp parallel for schedule(static)
+        for (long n = 0; n < N; n++) pfo_partition(C[n], phase + 3 * n, k9, c9, conc + 3 * n);
+#pragma omp parallel for schedule(static) collapse(2)
+        for (int sl = 0; sl < z; sl++)
+            for (int row = 0; row < y; row++)
+                for (int col = 0; col < x; col++) {
+                    const long n = col + (long)x * (row + (long)y * sl);
+                    long nbr[6] = {nb(col, x, -1) + (long)x * (row + (long)y * sl),
+                                   nb(col, x, 1) + (long)x * (row + (long)y * sl),
+                                   col + (long)x * (nb(row, y, -1) + (long)y * sl),
+                                   col + (long)x * (nb(row, y, 1) + (long)y * sl),
+                                   col + (long)x * (row + (long)y * nb(sl, z, -1)),
+                                   col + (long)x * (row + (long)y * nb(sl, z, 1))};
+                    double del = 0.;
+                    for (int ii = 0; ii < 6; ii++)
+                        for (int jj = 0; jj < 3; jj++)
+                            del += sqrt(phase[3 * nbr[ii] + jj] * phase[3 * n + jj]) *
+                                   (conc[3 * nbr[ii] + jj] - conc[3 * n + jj]) * D3[jj];
+                    C[n] += (del * dt_dxdx);
+                }
+    }
+    if (conc_out)
+        for (long n = 0; n < N; n++) pfo_partition(C[n], phase + 3 * n, k9, c9, conc_out + 3 * n);
+    free(conc);
+    return num_loop;
+}
+
+/* write_data.cpp:14-18 */
+void pfo_fractions(const pfo_model *m, const int32_t *ids, const double *phi, const double *phase,
+                   double *out4) {
+    const long N = (long)m->ix * m->iy * m->iz;
+    const double vol = (double)m->ix * m->iy * m->iz;
+    for (int p = 0; p < 3; p++) {
+        double s = 0.;
+        for (long n = 0; n < N; n++) s += phase[3 * n + p];
+        out4[p] = s / vol;
+    }
+    double s = 0.;
+    for (long e = 0; e < 6 * N; e++) s += (ids[e] < MAXGRAIN_PER_PHASE) ? phi[e] : 0.;
+    out4[3] = s / vol;
+}

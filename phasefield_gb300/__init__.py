@@ -1,0 +1,320 @@
+"""phasefield_gb300 -- GB300-native Steinbach multi-phase-field time step.
+
+The product is ``lib/libpfstep.so`` (hand-written sm_103a CUDA kernels behind a
+C ABI, ``include/pfstep.h``).  This module is a thin ctypes mirror of the
+reference's ``phase_field`` class (zhubq/PhaseField,
+C++-openmp-cuda/src/phase_field.h:20-120): ``read_data``, ``construct``,
+``update``, ``write_data``.  It does no arithmetic of its own and has no CPU
+fallback: if the library is missing every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libpfstep.so")
+CONFIG_DIR = os.path.join(_HERE, "configs")
+
+PF_OK = 0
+PF_ERR_ARG = -1
+PF_ERR_NOMEM = -2
+PF_ERR_CUDA = -3
+PF_ERR_TIMEOUT = -4
+PF_ERR_NONFINITE = -5
+PF_ERR_IO = -6
+PF_ERR_NODEV = -7
+PF_ERR_RANGE = -8
+PF_PREC_FP64 = 0
+PF_PREC_FP32C = 1
+PF_MAXT = 64
+
+_d9 = ctypes.c_double * 9
+_d3 = ctypes.c_double * 3
+
+
+class PfModel(ctypes.Structure):
+    """Mirror of ``pf_model`` (pfstep.h)."""
+
+    _fields_ = [
+        ("directory", ctypes.c_char * 256),
+        ("ix", ctypes.c_int), ("iy", ctypes.c_int), ("iz", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("i_intf", ctypes.c_int),
+        ("cutoff", ctypes.c_double),
+        ("num_grain", ctypes.c_int * 3),
+        ("phase_fraction", _d3),
+        ("init_conc", _d3),
+        ("nT", ctypes.c_int),
+        ("T_time", ctypes.c_double * PF_MAXT), ("T_temp", ctypes.c_double * PF_MAXT),
+        ("reduction", ctypes.c_double),
+        ("num_init_iteration", ctypes.c_int),
+        ("timestep_output", ctypes.c_double),
+        ("micro_out", ctypes.c_int),
+        ("num_nuclei", ctypes.c_double),
+        ("m0", _d9), ("mQ", _d9),
+        ("sigma", _d9),
+        ("D0", _d3 * 2), ("DQ", _d3 * 2),
+        ("thermo_file", ctypes.c_char * 256),
+        ("gpu_flag", ctypes.c_int),
+        ("nsol", ctypes.c_int),
+        ("mn_ratio", _d3),
+        ("ent_a", _d9), ("ent_b", _d9),
+        ("nple1_a", _d9), ("nple1_b", _d9), ("nple1_c", _d9),
+        ("nple2_a", _d9), ("nple2_b", _d9), ("nple2_c", _d9),
+        ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
+    ]
+
+
+class PfStepParams(ctypes.Structure):
+    """Mirror of ``pf_step_params`` (pfstep.h)."""
+
+    _fields_ = [
+        ("ix", ctypes.c_int), ("iy", ctypes.c_int), ("iz", ctypes.c_int),
+        ("nnb", ctypes.c_int), ("nsol", ctypes.c_int), ("n_sub", ctypes.c_int),
+        ("N", ctypes.c_longlong),
+        ("T", ctypes.c_double), ("time", ctypes.c_double),
+        ("dx", ctypes.c_double), ("cutoff", ctypes.c_double), ("eta", ctypes.c_double),
+        ("pfm_dt", ctypes.c_double), ("diff_dt", ctypes.c_double), ("dt_sub", ctypes.c_double),
+        ("factor1", ctypes.c_double), ("factor2", ctypes.c_double), ("factor3", ctypes.c_double),
+        ("coef_diff", ctypes.c_double),
+        ("m", _d9), ("sigma", _d9),
+        ("entropy", _d9), ("eq", _d9), ("dcdT", _d9),
+        ("D", _d3 * 2),
+        ("k", _d9 * 2), ("c", _d9 * 2),
+    ]
+
+
+class PfInitSpec(ctypes.Structure):
+    """Mirror of ``pf_init_spec`` (pfstep.h)."""
+
+    _fields_ = [
+        ("seed", ctypes.c_uint64),
+        ("n_grains", ctypes.c_int),
+        ("n_nuclei", ctypes.c_int),
+        ("nucleus_radius", ctypes.c_double),
+        ("n_particles", ctypes.c_int),
+        ("particle_radius", ctypes.c_double),
+        ("width", ctypes.c_double),
+        ("C0", ctypes.c_double * 2),
+        ("C_noise", ctypes.c_double * 2),
+        ("max_slots", ctypes.c_int),
+    ]
+
+
+# Every symbol pfstep.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+SYMBOLS = {
+    "GPU_Init": (_I, [_I, _I, _I]),
+    "GPU_Diffusion_solver": (None, [_DP, _DP, _DP, _DP, _DP, _I, _I, _I, _D, _D]),
+    "GPU_Cleanup": (None, []),
+    "pf_status_string": (ctypes.c_char_p, [_I]),
+    "pf_last_error": (ctypes.c_char_p, []),
+    "pf_abi_sizes": (_I, [ctypes.POINTER(ctypes.c_longlong)]),
+    "pf_model_read": (_I, [ctypes.c_char_p, ctypes.POINTER(PfModel)]),
+    "pf_thermo_read": (_I, [ctypes.c_char_p, ctypes.POINTER(PfModel)]),
+    "pf_params_at": (_I, [ctypes.POINTER(PfModel), _D, ctypes.POINTER(PfStepParams)]),
+    "pf_init_microstructure": (_I, [ctypes.POINTER(PfModel), ctypes.POINTER(PfInitSpec), _D, _P, _P, _P, _P, _P]),
+    "pf_create": (_I, [ctypes.POINTER(PfModel), _I, ctypes.POINTER(_P)]),
+    "pf_destroy": (_I, [_P]),
+    "pf_set_stream": (_I, [_P, _P]),
+    "pf_upload_state": (_I, [_P, _P, _P, _P, _P, _P, _D]),
+    "pf_download_state": (_I, [_P, _P, _P, _P, _P, _P, _DP]),
+    "pf_step": (_I, [_P, _I]),
+    "pf_reduce": (_I, [_P, _DP]),
+    "pf_synchronize": (_I, [_P]),
+    "pf_get_time": (_I, [_P, _DP]),
+    "pf_last_params": (_I, [_P, ctypes.POINTER(PfStepParams)]),
+    "pf_truncated_cells": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    "pf_enable_kernel_timing": (_I, [_P, _I]),
+    "pf_kernel_times": (_I, [_P, _DP, ctypes.POINTER(ctypes.c_longlong)]),
+    "pf_use_graph": (_I, [_P, _I]),
+    "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
+    "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libpfstep.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SYMBOLS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class PfError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        L = lib()
+        msg = f"{what}: {L.pf_status_string(status).decode()} ({L.pf_last_error().decode()})"
+        super().__init__(msg)
+        self.status = status
+
+
+def check(status: int, what: str) -> None:
+    if status != PF_OK:
+        raise PfError(status, what)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def read_model(config_path: str) -> PfModel:
+    m = PfModel()
+    check(lib().pf_model_read(config_path.encode(), ctypes.byref(m)), f"pf_model_read({config_path})")
+    return m
+
+
+def params_at(model: PfModel, time: float) -> PfStepParams:
+    p = PfStepParams()
+    check(lib().pf_params_at(ctypes.byref(model), time, ctypes.byref(p)), "pf_params_at")
+    return p
+
+
+def empty_state(model: PfModel) -> dict:
+    N = model.ix * model.iy * model.iz
+    return {
+        "ids": np.zeros(6 * N, np.int32),
+        "phi": np.zeros(6 * N, np.float64),
+        "phase": np.zeros(3 * N, np.float64),
+        "conc": np.zeros(3 * N * model.nsol, np.float64),
+        "C": np.zeros(N * model.nsol, np.float64),
+    }
+
+
+def init_microstructure(model: PfModel, spec: PfInitSpec, time: float) -> dict:
+    """Seeded initial state in the reference layout (host arrays)."""
+    st = empty_state(model)
+    check(lib().pf_init_microstructure(ctypes.byref(model), ctypes.byref(spec), time, _ptr(st["ids"]),
+                                       _ptr(st["phi"]), _ptr(st["phase"]), _ptr(st["conc"]), _ptr(st["C"])),
+          "pf_init_microstructure")
+    return st
+
+
+class PhaseField:
+    """Host-side mirror of the reference's ``phase_field`` object, running the
+    whole time step on the GPU through libpfstep."""
+
+    def __init__(self, model: PfModel, precision: int = PF_PREC_FP64):
+        self.model = model
+        self.precision = precision
+        self._ctx = ctypes.c_void_p()
+        check(lib().pf_create(ctypes.byref(model), precision, ctypes.byref(self._ctx)), "pf_create")
+
+    @classmethod
+    def read_data(cls, config_path: str, precision: int = PF_PREC_FP64) -> "PhaseField":
+        """phase_field::Read_data (phase_field.cpp:166-366)."""
+        return cls(read_model(config_path), precision)
+
+    @property
+    def N(self) -> int:
+        return self.model.ix * self.model.iy * self.model.iz
+
+    def close(self) -> None:
+        if self._ctx:
+            lib().pf_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, state: dict, time: float) -> None:
+        check(lib().pf_upload_state(self._ctx, _ptr(state["ids"]), _ptr(state["phi"]), _ptr(state["phase"]),
+                                    _ptr(state.get("conc")), _ptr(state["C"]), time), "pf_upload_state")
+
+    def construct(self, spec: PfInitSpec, time: float | None = None) -> dict:
+        """Seeded replacement of Construct + Nucleate1in2; uploads and returns the state."""
+        t = self.model.T_time[0] if time is None else time
+        st = init_microstructure(self.model, spec, t)
+        self.upload(st, t)
+        return st
+
+    def update(self, nsteps: int = 1) -> None:
+        """phase_field::Update(false) nsteps times (phase_field.cpp:243-305)."""
+        check(lib().pf_step(self._ctx, nsteps), "pf_step")
+
+    def synchronize(self) -> None:
+        check(lib().pf_synchronize(self._ctx), "pf_synchronize")
+
+    def download(self, conc: bool = True) -> dict:
+        st = empty_state(self.model)
+        t = ctypes.c_double()
+        check(lib().pf_download_state(self._ctx, _ptr(st["ids"]), _ptr(st["phi"]), _ptr(st["phase"]),
+                                      _ptr(st["conc"]) if conc else None, _ptr(st["C"]), ctypes.byref(t)),
+              "pf_download_state")
+        st["time"] = t.value
+        return st
+
+    def reduce(self) -> np.ndarray:
+        out = np.zeros(8, np.float64)
+        check(lib().pf_reduce(self._ctx, out.ctypes.data_as(_DP)), "pf_reduce")
+        return out
+
+    def fractions(self) -> np.ndarray:
+        """write_data.cpp:14-18: phase volume fractions and the deformed fraction."""
+        r = self.reduce()
+        return r[:4] / self.N
+
+    @property
+    def time(self) -> float:
+        t = ctypes.c_double()
+        check(lib().pf_get_time(self._ctx, ctypes.byref(t)), "pf_get_time")
+        return t.value
+
+    def last_params(self) -> PfStepParams:
+        p = PfStepParams()
+        check(lib().pf_last_params(self._ctx, ctypes.byref(p)), "pf_last_params")
+        return p
+
+    @property
+    def temperature(self) -> float:
+        return self.last_params().T
+
+    @property
+    def end_time(self) -> float:
+        return self.model.T_time[self.model.nT - 1]
+
+    def truncated_cells(self) -> int:
+        v = ctypes.c_longlong()
+        check(lib().pf_truncated_cells(self._ctx, ctypes.byref(v)), "pf_truncated_cells")
+        return v.value
+
+    def use_graph(self, on: bool = True) -> None:
+        check(lib().pf_use_graph(self._ctx, int(on)), "pf_use_graph")
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        check(lib().pf_set_stream(self._ctx, ctypes.c_void_p(stream_handle) if stream_handle else None),
+              "pf_set_stream")
+
+    def enable_kernel_timing(self, on: bool = True) -> None:
+        check(lib().pf_enable_kernel_timing(self._ctx, int(on)), "pf_enable_kernel_timing")
+
+    def kernel_times(self):
+        t = (ctypes.c_double * 2)()
+        n = (ctypes.c_longlong * 2)()
+        check(lib().pf_kernel_times(self._ctx, t, n), "pf_kernel_times")
+        return {"phase": (t[0], n[0]), "diffusion": (t[1], n[1])}
+
+    def write_data(self, directory: str | None = None, forced: bool = False) -> bool:
+        """phase_field::Write_data (write_data.cpp:3-40)."""
+        d = directory if directory is not None else self.model.directory.decode()
+        w = ctypes.c_int()
+        check(lib().pf_write_data(self._ctx, d.encode(), int(forced), ctypes.byref(w)), "pf_write_data")
+        return bool(w.value)

@@ -1,0 +1,627 @@
+// pf_api.cu -- the C ABI of libpfstep: the drop-in GPU_* plug-in and the
+// full-step pf_* context (state resident in HBM, kernels on one stream).
+//
+// Step orchestration follows phase_field::Update (zhubq/PhaseField,
+// C++-openmp-cuda/src/phase_field.cpp:243-305): evaluate the step's parameters
+// at the current time and advance time by pfm_dt (Update_parameter, :307-315),
+// one phase sweep into the second id/phi buffer and swap (:252-260), then
+// n_sub = max(ceil(pfm_dt/diff_dt),1) diffusion sub-steps of pfm_dt/n_sub,
+// swapping the concentration buffers after each (:408-418).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+#include "pf_dev.cuh"
+#include "pf_host.h"
+#include "pf_kernels.h"
+
+static int pf_cuda_fail(cudaError_t e) {
+    return pf_fail(PF_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+}
+
+// ===========================================================================
+// 1. Drop-in for gpu_solver.h (module state, single host thread, like the
+//    reference's statics in gpu_solver.cpp:13-18).
+// ===========================================================================
+namespace {
+struct DropIn {
+    int x = 0, y = 0, z = 0;
+    double *phase = nullptr, *C = nullptr, *conc[2] = {nullptr, nullptr};
+    bool ready = false;
+} g_drop;
+
+void dropin_free() {
+    cudaFree(g_drop.phase);
+    cudaFree(g_drop.C);
+    cudaFree(g_drop.conc[0]);
+    cudaFree(g_drop.conc[1]);
+    g_drop = DropIn();
+}
+}  // namespace
+
+extern "C" int GPU_Init(const int x, const int y, const int z) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (cudaSetDevice(0) != cudaSuccess) return 0;
+    if (x < 1 || y < 1 || z < 1) return 0;
+    if (g_drop.ready) dropin_free();
+    const size_t N = (size_t)x * y * z;
+    size_t freeb = 0, total = 0;
+    cudaMemGetInfo(&freeb, &total);
+    if (N * sizeof(double) * 10 > freeb) return 0;
+    if (cudaMalloc(&g_drop.phase, 3 * N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&g_drop.C, N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&g_drop.conc[0], 3 * N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&g_drop.conc[1], 3 * N * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        dropin_free();
+        return 0;
+    }
+    g_drop.x = x; g_drop.y = y; g_drop.z = z;
+    g_drop.ready = true;
+    return 1;
+}
+
+extern "C" void GPU_Diffusion_solver(double *hdiffusivity, double *hpartition_k, double *hpartition_c,
+                                     double *hvalue_phase, double *htotal_conc, int x, int y, int z,
+                                     double dt, double dx) {
+    if (!g_drop.ready || x != g_drop.x || y != g_drop.y || z != g_drop.z) {
+        if (!GPU_Init(x, y, z)) {
+            pf_fail(PF_ERR_NODEV, "GPU_Diffusion_solver: GPU_Init failed");
+            return;
+        }
+    }
+    const long long N = (long long)x * y * z;
+    pf_step_params P;
+    std::memset(&P, 0, sizeof(P));
+    P.ix = x; P.iy = y; P.iz = z; P.N = N; P.nsol = 1;
+    for (int p = 0; p < 3; p++) P.D[0][p] = hdiffusivity[p];
+    for (int e = 0; e < 9; e++) {
+        P.k[0][e] = hpartition_k[e];
+        P.c[0][e] = hpartition_c[e];
+    }
+    // gpu_solver.cpp:93-94, 206-209 (0.2f kept: it decides num_loop).
+    const int dims = z > 1 ? 3 : 2;
+    double max_diff = hdiffusivity[0];
+    for (int p = 1; p < 3; p++)
+        if (hdiffusivity[p] > max_diff) max_diff = hdiffusivity[p];
+    const double del_t = dx * dx / max_diff / dims * 0.2f;
+    const int num_loop = (int)std::ceil(dt / del_t);
+    const double dt_dxdx = dt / num_loop / (dx * dx);
+    cudaStream_t s = 0;
+    cudaMemcpy(g_drop.phase, hvalue_phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(g_drop.C, htotal_conc, N * sizeof(double), cudaMemcpyHostToDevice);
+    pf_launch_partition_f64(P, g_drop.phase, g_drop.C, g_drop.conc[0], s);
+    int a = 0;
+    for (int it = 1; it <= num_loop; it++) {
+        pf_launch_diffuse_f64(P, 6, dt_dxdx, g_drop.phase, g_drop.conc[a], g_drop.conc[1 - a], g_drop.C, s);
+        a = 1 - a;
+    }
+    cudaError_t e = cudaMemcpy(htotal_conc, g_drop.C, N * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) pf_cuda_fail(e);
+}
+
+extern "C" void GPU_Cleanup(void) {
+    if (g_drop.ready) dropin_free();
+}
+
+// ===========================================================================
+// 2. Full-step context.
+// ===========================================================================
+struct pf_ctx {
+    pf_model model;
+    int prec = PF_PREC_FP64;
+    long long N = 0;
+    int nsol = 1;
+    double time = 0.;
+    bool have_state = false;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // FP64 reference layout
+    int *ids[2] = {nullptr, nullptr};
+    double *phi[2] = {nullptr, nullptr};
+    double *phase = nullptr;
+    double *conc[2] = {nullptr, nullptr};
+    double *C = nullptr;
+    int cur = 0, curc = 0;
+    // FP32 compact layout
+    ushort4 *gid[2] = {nullptr, nullptr};
+    float4 *phi32[2] = {nullptr, nullptr};
+    float *phase32 = nullptr;
+    float2 *sol[2] = {nullptr, nullptr};
+    int curs = 0;
+    pf_f32_map map{};
+    int *d_span = nullptr;
+    unsigned int *d_trunc = nullptr;
+    long long truncated = 0;
+    // reductions
+    double *partials = nullptr;
+    int red_blocks = 0;
+    double *d_red = nullptr;
+    double *h_red = nullptr;  // pinned
+    // per-step bookkeeping
+    pf_step_params last{};
+    bool have_last = false;
+    double last_temperature_written = 0.;
+    int micro_count = 0;
+    // kernel timing
+    bool ktiming = false;
+    std::vector<cudaEvent_t> ev_free;
+    struct Pending { cudaEvent_t a, b; int kind; };
+    std::vector<Pending> pending;
+    double ktime[2] = {0., 0.};
+    long long kcount[2] = {0, 0};
+    // graphs
+    bool use_graph = false;
+    cudaGraphExec_t gexec = nullptr;
+    pf_step_params gparams{};
+    int gphase = -1;
+};
+
+namespace {
+
+cudaEvent_t ev_get(pf_ctx *c) {
+    if (!c->ev_free.empty()) {
+        cudaEvent_t e = c->ev_free.back();
+        c->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int collect_times(pf_ctx *c) {
+    if (c->pending.empty()) return PF_OK;
+    PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    for (auto &p : c->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        c->ktime[p.kind] += ms;
+        c->kcount[p.kind] += 1;
+        c->ev_free.push_back(p.a);
+        c->ev_free.push_back(p.b);
+    }
+    c->pending.clear();
+    return PF_OK;
+}
+
+template <class F>
+cudaError_t timed(pf_ctx *c, int kind, F launch) {
+    if (!c->ktiming) return launch();
+    cudaEvent_t a = ev_get(c), b = ev_get(c);
+    cudaEventRecord(a, c->stream);
+    cudaError_t e = launch();
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({a, b, kind});
+    if (c->pending.size() > 4096) collect_times(c);
+    return e;
+}
+
+void free_all(pf_ctx *c) {
+    for (int i = 0; i < 2; i++) {
+        cudaFree(c->ids[i]); cudaFree(c->phi[i]); cudaFree(c->conc[i]);
+        cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
+    }
+    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->phase32);
+    cudaFree(c->d_span); cudaFree(c->d_trunc);
+    cudaFree(c->partials); cudaFree(c->d_red);
+    if (c->h_red) cudaFreeHost(c->h_red);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : c->ev_free) cudaEventDestroy(e);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+}
+
+// Launch one full step with parameters P (no parameter evaluation, no time
+// update).  Buffer roles advance.
+cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
+    cudaError_t e = cudaSuccess;
+    if (c->prec == PF_PREC_FP64) {
+        const int a = c->cur;
+        e = timed(c, 0, [&] {
+            return pf_launch_phase_f64(P, c->ids[a], c->phi[a], c->ids[1 - a], c->phi[1 - a], c->phase,
+                                       c->conc[c->curc], c->C, c->stream);
+        });
+        if (e != cudaSuccess) return e;
+        c->cur = 1 - a;
+        for (int it = 0; it < P.n_sub; it++) {
+            const int b = c->curc;
+            e = timed(c, 1, [&] {
+                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->phase, c->conc[b], c->conc[1 - b], c->C,
+                                             c->stream);
+            });
+            if (e != cudaSuccess) return e;
+            c->curc = 1 - b;
+        }
+    } else {
+        pf_f32_params F;
+        pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
+        const int a = c->cur;
+        e = timed(c, 0, [&] {
+            return pf_launch_phase_f32(F, c->gid[a], c->phi32[a], c->gid[1 - a], c->phi32[1 - a], c->phase32,
+                                       c->sol[c->curs], c->stream);
+        });
+        if (e != cudaSuccess) return e;
+        c->cur = 1 - a;
+        for (int it = 0; it < P.n_sub; it++) {
+            const int b = c->curs;
+            e = timed(c, 1, [&] {
+                return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream);
+            });
+            if (e != cudaSuccess) return e;
+            c->curs = 1 - b;
+        }
+    }
+    return e;
+}
+
+bool same_step(const pf_step_params &a, const pf_step_params &b) {
+    pf_step_params x = a, y = b;
+    x.time = y.time = 0.;
+    return std::memcmp(&x, &y, sizeof(x)) == 0;
+}
+
+// Buffer-role signature: graphs are captured for a fixed assignment.
+int role_sig(const pf_ctx *c) { return c->cur | (c->curc << 1) | (c->curs << 2); }
+
+}  // namespace
+
+extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
+    if (!model || !out) return pf_fail(PF_ERR_ARG, "pf_create: null argument");
+    *out = nullptr;
+    if (precision != PF_PREC_FP64 && precision != PF_PREC_FP32C) return pf_fail(PF_ERR_ARG, "pf_create: bad precision");
+    if (model->ix < 1 || model->iy < 1 || model->iz < 1 || model->nsol < 1 || model->nsol > 2 || model->nT < 1)
+        return pf_fail(PF_ERR_ARG, "pf_create: bad model");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return pf_fail(PF_ERR_NODEV, "pf_create: no CUDA device");
+    }
+    pf_ctx *c = new pf_ctx();
+    c->model = *model;
+    c->prec = precision;
+    c->N = (long long)model->ix * model->iy * model->iz;
+    c->nsol = model->nsol;
+    const size_t N = (size_t)c->N;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return pf_cuda_fail(e); }
+    c->own_stream = true;
+    bool ok = true;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (ok && cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+    };
+    if (precision == PF_PREC_FP64) {
+        for (int i = 0; i < 2; i++) {
+            alloc((void **)&c->ids[i], 6 * N * sizeof(int));
+            alloc((void **)&c->phi[i], 6 * N * sizeof(double));
+            alloc((void **)&c->conc[i], 3 * N * c->nsol * sizeof(double));
+        }
+        alloc((void **)&c->phase, 3 * N * sizeof(double));
+        alloc((void **)&c->C, N * c->nsol * sizeof(double));
+    } else {
+        for (int i = 0; i < 2; i++) {
+            alloc((void **)&c->gid[i], N * sizeof(ushort4));
+            alloc((void **)&c->phi32[i], N * sizeof(float4));
+            alloc((void **)&c->sol[i], N * c->nsol * sizeof(float2));
+        }
+        alloc((void **)&c->phase32, 3 * N * sizeof(float));
+        alloc((void **)&c->d_span, 8 * sizeof(int));
+        alloc((void **)&c->d_trunc, sizeof(unsigned int));
+    }
+    c->red_blocks = pf_reduce_blocks(c->N);
+    alloc((void **)&c->partials, (size_t)c->red_blocks * PF_RED_NOUT * sizeof(double));
+    alloc((void **)&c->d_red, PF_RED_NOUT * sizeof(double));
+    if (ok && cudaMallocHost((void **)&c->h_red, PF_RED_NOUT * sizeof(double)) != cudaSuccess) ok = false;
+    if (!ok) {
+        cudaGetLastError();
+        free_all(c);
+        delete c;
+        return pf_fail(PF_ERR_NOMEM, "pf_create: device allocation failed");
+    }
+    *out = c;
+    return PF_OK;
+}
+
+extern "C" int pf_destroy(pf_ctx *c) {
+    if (!c) return PF_OK;
+    cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return PF_OK;
+}
+
+extern "C" int pf_set_stream(pf_ctx *c, void *stream) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_set_stream: null context");
+    PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+        c->own_stream = false;
+    } else {
+        PF_CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    return PF_OK;
+}
+
+extern "C" int pf_upload_state(pf_ctx *c, const int32_t *ids, const double *phi, const double *phase,
+                               const double *conc, const double *C, double time) {
+    if (!c || !ids || !phi || !phase || !C) return pf_fail(PF_ERR_ARG, "pf_upload_state: null argument");
+    const size_t N = (size_t)c->N;
+    c->time = time;
+    c->cur = c->curc = c->curs = 0;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    pf_step_params P;
+    pf_compute_params(c->model, time, P);
+    if (c->prec == PF_PREC_FP64) {
+        PF_CUDA_OK(cudaMemcpyAsync(c->ids[0], ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+        PF_CUDA_OK(cudaMemcpyAsync(c->phi[0], phi, 6 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PF_CUDA_OK(cudaMemcpyAsync(c->phase, phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PF_CUDA_OK(cudaMemcpyAsync(c->C, C, N * c->nsol * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        if (conc)
+            PF_CUDA_OK(cudaMemcpyAsync(c->conc[0], conc, 3 * N * c->nsol * sizeof(double), cudaMemcpyHostToDevice,
+                                       c->stream));
+        else
+            PF_CUDA_OK(pf_launch_partition_f64(P, c->phase, c->C, c->conc[0], c->stream));
+    } else {
+        // Stage the reference layout in the (not yet used) second buffers'
+        // space: FP64 staging buffers are allocated for the duration of the
+        // upload only.
+        int *d_ids = nullptr;
+        double *d_phi = nullptr, *d_phase = nullptr, *d_C = nullptr;
+        bool ok = cudaMalloc(&d_ids, 6 * N * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&d_phi, 6 * N * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&d_phase, 3 * N * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&d_C, N * c->nsol * sizeof(double)) == cudaSuccess;
+        int st = PF_OK;
+        if (!ok) {
+            cudaGetLastError();
+            st = pf_fail(PF_ERR_NOMEM, "pf_upload_state: staging allocation failed");
+        }
+        cudaError_t e = cudaSuccess;
+        if (st == PF_OK) {
+            cudaMemcpyAsync(d_ids, ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(d_phi, phi, 6 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(d_phase, phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+            cudaMemcpyAsync(d_C, C, N * c->nsol * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+            cudaMemsetAsync(c->d_span, 0, 8 * sizeof(int), c->stream);
+            cudaMemsetAsync(c->d_trunc, 0, sizeof(unsigned int), c->stream);
+            pf_launch_id_span(d_ids, c->N, c->d_span, c->stream);
+            int span[8];
+            e = cudaMemcpyAsync(span, c->d_span, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) st = pf_cuda_fail(e);
+            else if (span[4] != 0) st = pf_fail(PF_ERR_RANGE, "pf_upload_state: grain id outside 0..399999");
+            else {
+                c->map.off[0] = 0;
+                c->map.off[1] = span[0];
+                c->map.off[2] = span[0] + span[1];
+                c->map.off[3] = span[0] + span[1] + span[2];
+                c->map.total = c->map.off[3] + span[3];
+                if (c->map.total > 65535) st = pf_fail(PF_ERR_RANGE, "pf_upload_state: more than 65535 grains");
+            }
+            if (st == PF_OK) {
+                e = pf_launch_pack_f32(c->N, c->nsol, c->map, d_ids, d_phi, d_phase, d_C, c->gid[0], c->phi32[0],
+                                       c->phase32, c->sol[0], c->d_trunc, c->stream);
+                unsigned int tr = 0;
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(&tr, c->d_trunc, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+                if (e != cudaSuccess) st = pf_cuda_fail(e);
+                c->truncated = tr;
+            }
+        }
+        cudaStreamSynchronize(c->stream);
+        cudaFree(d_ids); cudaFree(d_phi); cudaFree(d_phase); cudaFree(d_C);
+        if (st != PF_OK) return st;
+    }
+    c->have_state = true;
+    c->have_last = false;
+    return PF_OK;
+}
+
+extern "C" int pf_download_state(pf_ctx *c, int32_t *ids, double *phi, double *phase, double *conc, double *C,
+                                 double *time) {
+    if (!c || !c->have_state) return pf_fail(PF_ERR_ARG, "pf_download_state: no state");
+    const size_t N = (size_t)c->N;
+    if (time) *time = c->time;
+    if (c->prec == PF_PREC_FP64) {
+        if (ids) PF_CUDA_OK(cudaMemcpyAsync(ids, c->ids[c->cur], 6 * N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        if (phi) PF_CUDA_OK(cudaMemcpyAsync(phi, c->phi[c->cur], 6 * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (phase) PF_CUDA_OK(cudaMemcpyAsync(phase, c->phase, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (conc)
+            PF_CUDA_OK(cudaMemcpyAsync(conc, c->conc[c->curc], 3 * N * c->nsol * sizeof(double), cudaMemcpyDeviceToHost,
+                                       c->stream));
+        if (C) PF_CUDA_OK(cudaMemcpyAsync(C, c->C, N * c->nsol * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+        return PF_OK;
+    }
+    int *d_ids = nullptr;
+    double *d_phi = nullptr, *d_phase = nullptr, *d_conc = nullptr, *d_C = nullptr;
+    bool ok = cudaMalloc(&d_ids, 6 * N * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&d_phi, 6 * N * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&d_phase, 3 * N * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&d_C, N * c->nsol * sizeof(double)) == cudaSuccess &&
+              (!conc || cudaMalloc(&d_conc, 3 * N * c->nsol * sizeof(double)) == cudaSuccess);
+    int st = PF_OK;
+    if (!ok) {
+        cudaGetLastError();
+        st = pf_fail(PF_ERR_NOMEM, "pf_download_state: staging allocation failed");
+    } else {
+        pf_step_params P;
+        pf_compute_params(c->model, c->time, P);
+        cudaError_t e = pf_launch_unpack_f32(P, c->map, c->gid[c->cur], c->phi32[c->cur], c->phase32, c->sol[c->curs],
+                                             d_ids, d_phi, d_phase, d_conc, d_C, c->stream);
+        if (e == cudaSuccess && ids) e = cudaMemcpyAsync(ids, d_ids, 6 * N * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && phi) e = cudaMemcpyAsync(phi, d_phi, 6 * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && phase)
+            e = cudaMemcpyAsync(phase, d_phase, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && conc)
+            e = cudaMemcpyAsync(conc, d_conc, 3 * N * c->nsol * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && C) e = cudaMemcpyAsync(C, d_C, N * c->nsol * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) st = pf_cuda_fail(e);
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d_ids); cudaFree(d_phi); cudaFree(d_phase); cudaFree(d_conc); cudaFree(d_C);
+    return st;
+}
+
+extern "C" int pf_step(pf_ctx *c, int nsteps) {
+    if (!c || !c->have_state) return pf_fail(PF_ERR_ARG, "pf_step: no state uploaded");
+    if (nsteps < 0) return pf_fail(PF_ERR_ARG, "pf_step: negative step count");
+    int s = 0;
+    while (s < nsteps) {
+        pf_step_params P;
+        pf_compute_params(c->model, c->time, P);
+        // Graph path: two steps with identical parameters return every buffer
+        // to its role, so one captured pair is replayed.
+        if (c->use_graph && !c->ktiming && s + 1 < nsteps) {
+            pf_step_params P2;
+            pf_compute_params(c->model, c->time + P.pfm_dt, P2);
+            if (same_step(P, P2)) {
+                const int sig = role_sig(c);
+                if (!c->gexec || c->gphase != sig || !same_step(c->gparams, P)) {
+                    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+                    cudaGraph_t g;
+                    PF_CUDA_OK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                    cudaError_t e1 = launch_step(c, P);
+                    cudaError_t e2 = launch_step(c, P2);
+                    cudaError_t e3 = cudaStreamEndCapture(c->stream, &g);
+                    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+                        return pf_cuda_fail(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3));
+                    cudaError_t e4 = cudaGraphInstantiate(&c->gexec, g, 0);
+                    cudaGraphDestroy(g);
+                    if (e4 != cudaSuccess) return pf_cuda_fail(e4);
+                    c->gparams = P;
+                    c->gphase = sig;  // roles are back where they started after two steps
+                }
+                PF_CUDA_OK(cudaGraphLaunch(c->gexec, c->stream));
+                c->time += P.pfm_dt;
+                c->time += P2.pfm_dt;
+                c->last = P2;
+                c->have_last = true;
+                s += 2;
+                continue;
+            }
+        }
+        cudaError_t e = launch_step(c, P);
+        if (e != cudaSuccess) return pf_cuda_fail(e);
+        c->time += P.pfm_dt;  // phase_field.cpp:314
+        c->last = P;
+        c->have_last = true;
+        s += 1;
+    }
+    return PF_OK;
+}
+
+extern "C" int pf_reduce(pf_ctx *c, double out[8]) {
+    if (!c || !c->have_state || !out) return pf_fail(PF_ERR_ARG, "pf_reduce: no state");
+    cudaError_t e;
+    if (c->prec == PF_PREC_FP64)
+        e = pf_launch_reduce_f64(c->N, c->nsol, c->ids[c->cur], c->phi[c->cur], c->phase, c->C, c->partials,
+                                 c->red_blocks, c->d_red, c->stream);
+    else
+        e = pf_launch_reduce_f32(c->N, c->nsol, c->map.off[1], c->gid[c->cur], c->phi32[c->cur], c->phase32,
+                                 c->sol[c->curs], c->partials, c->red_blocks, c->d_red, c->stream);
+    if (e != cudaSuccess) return pf_cuda_fail(e);
+    PF_CUDA_OK(cudaMemcpyAsync(c->h_red, c->d_red, PF_RED_NOUT * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < PF_RED_NOUT; i++) out[i] = c->h_red[i];
+    out[6] = 0.;
+    if (c->nsol < 2) out[5] = 0.;
+    return PF_OK;
+}
+
+extern "C" int pf_synchronize(pf_ctx *c) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_synchronize: null context");
+    PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+extern "C" int pf_get_time(pf_ctx *c, double *t) {
+    if (!c || !t) return pf_fail(PF_ERR_ARG, "pf_get_time: null argument");
+    *t = c->time;
+    return PF_OK;
+}
+
+extern "C" int pf_last_params(pf_ctx *c, pf_step_params *out) {
+    if (!c || !out) return pf_fail(PF_ERR_ARG, "pf_last_params: null argument");
+    if (c->have_last) *out = c->last;
+    else pf_compute_params(c->model, c->time, *out);
+    return PF_OK;
+}
+
+extern "C" int pf_truncated_cells(pf_ctx *c, long long *out) {
+    if (!c || !out) return pf_fail(PF_ERR_ARG, "pf_truncated_cells: null argument");
+    *out = c->truncated;
+    return PF_OK;
+}
+
+extern "C" int pf_enable_kernel_timing(pf_ctx *c, int on) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_enable_kernel_timing: null context");
+    int st = collect_times(c);
+    c->ktiming = on != 0;
+    c->ktime[0] = c->ktime[1] = 0.;
+    c->kcount[0] = c->kcount[1] = 0;
+    return st;
+}
+
+extern "C" int pf_kernel_times(pf_ctx *c, double times_ms[2], long long counts[2]) {
+    if (!c || !times_ms || !counts) return pf_fail(PF_ERR_ARG, "pf_kernel_times: null argument");
+    int st = collect_times(c);
+    for (int i = 0; i < 2; i++) {
+        times_ms[i] = c->ktime[i];
+        counts[i] = c->kcount[i];
+    }
+    return st;
+}
+
+extern "C" int pf_use_graph(pf_ctx *c, int on) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_use_graph: null context");
+    c->use_graph = on != 0;
+    return PF_OK;
+}
+
+extern "C" int pf_write_data(pf_ctx *c, const char *directory, int forced, int *written) {
+    if (!c || !directory) return pf_fail(PF_ERR_ARG, "pf_write_data: null argument");
+    if (written) *written = 0;
+    pf_step_params P;
+    pf_last_params(c, &P);
+    const double temperature = P.T;
+    if (!(forced || pf_output_due(c->time, c->model.timestep_output, P.pfm_dt, temperature,
+                                  c->last_temperature_written)))
+        return PF_OK;
+    double r[8];
+    int st = pf_reduce(c, r);
+    if (st != PF_OK) return st;
+    const double vol = (double)c->model.ix * c->model.iy * c->model.iz;
+    double fr[3] = {r[0] / vol, r[1] / vol, r[2] / vol};
+    std::string line = pf_format_fraction_line(c->time, temperature, fr, r[3] / vol);
+    std::ofstream k(std::string(directory) + "/fraction_time.txt", std::ios::app);
+    if (!k.is_open()) return pf_fail(PF_ERR_IO, "pf_write_data: cannot open fraction_time.txt");
+    k << line;
+    if (c->model.micro_out) {
+        const size_t N = (size_t)c->N;
+        std::vector<int32_t> ids(6 * N);
+        std::vector<double> C(N * c->nsol);
+        st = pf_download_state(c, ids.data(), nullptr, nullptr, nullptr, C.data(), nullptr);
+        if (st != PF_OK) return st;
+        char name[64];
+        std::snprintf(name, sizeof(name), "field%07d_%d.vti", (int)(c->time * 100), c->micro_count);
+        st = pf_write_vti((std::string(directory) + "/" + name).c_str(), c->model.ix, c->model.iy, c->model.iz,
+                          c->model.dx, ids.data(), C.data());
+        if (st != PF_OK) return st;
+        c->micro_count++;
+    }
+    c->last_temperature_written = temperature;
+    if (written) *written = 1;
+    return PF_OK;
+}

@@ -1,0 +1,42 @@
+// pf_dev.cuh -- small device helpers shared by the FP64 and FP32 kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "pf_types.h"
+
+// Periodic neighbour (phase_field.h:58-68 restated 0-based; also gpu_solver.cpp:123-126).
+__device__ __forceinline__ int pf_wrap(int i, int len, int d) {
+    int g = i + d;
+    if (g >= len) g -= len;
+    else if (g < 0) g += len;
+    return g;
+}
+
+// phase_field.h:25-29: grain id -> phase (0 for an empty slot).
+__device__ __forceinline__ int pf_phase_of_grain(int g) {
+    if (g == 0) return 0;
+    int q = g / PF_MAXGRAIN_PER_PHASE;
+    return q > 0 ? q : 1;
+}
+
+// Neighbour linear indices in the reference order x-, x+, y-, y+, z-, z+
+// (solver.cpp:159-166, :353-358).
+__device__ __forceinline__ void pf_neighbours(long long n, int ix, int iy, int iz, long long nbr[6]) {
+    const int i = (int)(n % ix);
+    const long long r = n / ix;
+    const int j = (int)(r % iy);
+    const int k = (int)(r / iy);
+    const long long plane = (long long)ix * iy;
+    nbr[0] = pf_wrap(i, ix, -1) + (long long)ix * j + plane * k;
+    nbr[1] = pf_wrap(i, ix, 1) + (long long)ix * j + plane * k;
+    nbr[2] = i + (long long)ix * pf_wrap(j, iy, -1) + plane * k;
+    nbr[3] = i + (long long)ix * pf_wrap(j, iy, 1) + plane * k;
+    nbr[4] = i + (long long)ix * j + plane * pf_wrap(k, iz, -1);
+    nbr[5] = i + (long long)ix * j + plane * pf_wrap(k, iz, 1);
+}
+
+#define PF_CUDA_OK(call)                                  \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return pf_cuda_fail(e_);   \
+    } while (0)

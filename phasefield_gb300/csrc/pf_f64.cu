@@ -1,0 +1,340 @@
+// pf_f64.cu -- plain FP64 step kernels in the reference layout (sm_103a).
+//
+// These kernels are the parity path: they evaluate every floating-point
+// operation of the reference's CPU solver (zhubq/PhaseField,
+// C++-openmp-cuda/src/solver.cpp) in the same order, and this file is compiled
+// with -fmad=false so that no multiply-add is contracted.  IEEE sqrt and
+// division are correctly rounded on the device, so the results are
+// bit-identical to a -ffp-contract=off host build of the same arithmetic.
+//
+// Layout (phase_field.h:81-89): slot/phase fastest, then x, y, z.
+//   ids[6n+s] int32, phi[6n+s] f64, phase[3n+p] f64,
+//   conc[q*3N + 3n+p] f64, C[q*N + n] f64.
+#include "pf_dev.cuh"
+#include "pf_kernels.h"
+
+namespace {
+
+// Driving_force (solver.cpp:374-387) for a phase pair, given the cell's carbon
+// concentration of phase pi.  df = 0.; df += ... is kept literally.
+__device__ __forceinline__ double pf_df(const pf_step_params &P, int pi, int pj, double conc_pi) {
+    double df = 0.;
+    if (pi != pj) {
+        const int e = (pi - 1) + 3 * (pj - 1);
+        df += P.entropy[e] * (conc_pi - P.eq[e]) / P.dcdT[e];
+    }
+    return df;
+}
+
+// solver.cpp:389-405
+__device__ __forceinline__ void pf_partition(double C, const double ph[3], const double *k9,
+                                             const double *c9, double out[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        double t1 = 0., t2 = 0.;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            t1 += ph[j] * k9[i + 3 * j];
+            t2 += ph[j] * c9[i + 3 * j];
+        }
+        out[i] = (C - t2) / t1;
+    }
+}
+
+// Phase_field_solver (solver.cpp:147-304), one thread per cell.
+__global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P,
+                                                   const int *__restrict__ ids1,
+                                                   const double *__restrict__ phi1,
+                                                   int *__restrict__ ids2, double *__restrict__ phi2,
+                                                   double *__restrict__ phase,
+                                                   double *__restrict__ conc1,
+                                                   const double *__restrict__ C) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    long long nbr[6];
+    pf_neighbours(n, P.ix, P.iy, P.iz, nbr);
+    const double cutoff = P.cutoff;
+
+    // 1-based stencil arrays of the reference become 0-based position arrays.
+    int sid[PF_NSTENCIL], sph[PF_NSTENCIL];
+    double s1[PF_NSTENCIL], s2[PF_NSTENCIL];
+#pragma unroll
+    for (int a = 0; a < PF_NSTENCIL; a++) {
+        sid[a] = 0; sph[a] = 0; s1[a] = 0.; s2[a] = 0.;
+    }
+    int own_id[6];
+    double own_v[6];
+    {
+        const int2 *ip = reinterpret_cast<const int2 *>(ids1 + 6 * n);
+        const double2 *vp = reinterpret_cast<const double2 *>(phi1 + 6 * n);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            int2 t = __ldg(ip + a);
+            double2 v = __ldg(vp + a);
+            own_id[2 * a] = t.x; own_id[2 * a + 1] = t.y;
+            own_v[2 * a] = v.x; own_v[2 * a + 1] = v.y;
+        }
+    }
+    // solver.cpp:168-175: own slots above the cutoff keep their slot position.
+    int num = 0;
+#pragma unroll
+    for (int a = 0; a < 6; a++) {
+        if (own_v[a] > cutoff) {
+            num += 1;
+            sid[a] = own_id[a];
+            sph[a] = pf_phase_of_grain(own_id[a]);
+            s1[a] = own_v[a];
+        }
+    }
+    // solver.cpp:179-205: merge the neighbours' lists, stopping at id 0.
+#pragma unroll
+    for (int b = 0; b < 6; b++) {
+        if (b < P.nnb) {
+            const long long q = nbr[b];
+            int nid[6];
+            double nv[6];
+            const int2 *ip = reinterpret_cast<const int2 *>(ids1 + 6 * q);
+            const double2 *vp = reinterpret_cast<const double2 *>(phi1 + 6 * q);
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                int2 t = __ldg(ip + a);
+                double2 v = __ldg(vp + a);
+                nid[2 * a] = t.x; nid[2 * a + 1] = t.y;
+                nv[2 * a] = v.x; nv[2 * a + 1] = v.y;
+            }
+            bool live = true;
+#pragma unroll
+            for (int a = 0; a < 6; a++) {
+                const int tid = nid[a];
+                live = live && (tid != 0);
+                if (live) {
+                    bool found = false;
+#pragma unroll
+                    for (int kk = 0; kk < PF_NSTENCIL; kk++) {
+                        if (!found && tid == sid[kk]) {
+                            s2[kk] += nv[a];
+                            found = true;
+                        }
+                    }
+                    if (!found && num < PF_NSTENCIL) {
+#pragma unroll
+                        for (int kk = 0; kk < PF_NSTENCIL; kk++) {
+                            if (kk == num) {
+                                sid[kk] = tid;
+                                sph[kk] = pf_phase_of_grain(tid);
+                                s2[kk] += nv[a];
+                            }
+                        }
+                        num += 1;
+                    }
+                }
+            }
+        }
+    }
+    // solver.cpp:207-216: a single field in the stencil -> copy and return.
+    if (num == 1) {
+        int2 *op = reinterpret_cast<int2 *>(ids2 + 6 * n);
+        double2 *ov = reinterpret_cast<double2 *>(phi2 + 6 * n);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            op[a] = make_int2(own_id[2 * a], own_id[2 * a + 1]);
+            ov[a] = make_double2(own_v[2 * a], own_v[2 * a + 1]);
+        }
+        return;
+    }
+    // Driving forces depend only on the phase pair and the cell's carbon
+    // concentration (solver.cpp:231-232, 374-387): evaluate the six ordered
+    // off-diagonal pairs once.
+    double lc[3];
+    lc[0] = conc1[3 * n + 0]; lc[1] = conc1[3 * n + 1]; lc[2] = conc1[3 * n + 2];
+    double df[9];
+#pragma unroll
+    for (int a = 1; a <= 3; a++)
+#pragma unroll
+        for (int b = 1; b <= 3; b++) df[(a - 1) + 3 * (b - 1)] = pf_df(P, a, b, lc[a - 1]);
+
+    const double factor1 = P.factor1, factor2 = P.factor2, factor3 = P.factor3;
+    double del[PF_NSTENCIL];
+#pragma unroll
+    for (int ii = 0; ii < PF_NSTENCIL; ii++) {
+        del[ii] = 0.;
+        if (ii < num) {
+            const int pi = sph[ii];
+#pragma unroll
+            for (int jj = 0; jj < PF_NSTENCIL; jj++) {
+                if (jj < num && jj != ii) {
+                    const int pj = sph[jj];
+                    if (abs(pi - pj) != 2) {
+                        const int e = (pi - 1) + 3 * (pj - 1);
+                        double d = 0.;
+                        d = (s2[ii] * s1[jj] - s2[jj] * s1[ii]) * factor1;
+                        d += (s1[ii] - s1[jj]) * factor2;
+                        d *= P.sigma[e];
+                        double dfe = 0.;
+#pragma unroll
+                        for (int t = 0; t < 9; t++)
+                            if (t == e) dfe = df[t];
+                        d += factor3 * sqrt(s1[ii] * s1[jj]) * dfe;
+                        d *= P.m[e];
+                        del[ii] += d;
+                    }
+                }
+            }
+            del[ii] *= P.pfm_dt;
+            del[ii] += s1[ii];
+            if (del[ii] > 1.0) del[ii] = 1.0;
+            else if (del[ii] < cutoff) del[ii] = 0.;
+        }
+    }
+    // Sort_xyz (solver.cpp:426-432): selection sort, first maximum wins.  Only
+    // the first six positions are read afterwards.
+#pragma unroll
+    for (int a = 0; a < PF_NSLOT64; a++) {
+        int mx = a;
+        double mv = del[a];
+#pragma unroll
+        for (int b = a + 1; b < PF_NSTENCIL; b++) {
+            if (del[b] > mv) { mv = del[b]; mx = b; }
+        }
+#pragma unroll
+        for (int b = a + 1; b < PF_NSTENCIL; b++) {
+            if (b == mx) {
+                double tv = del[a]; del[a] = del[b]; del[b] = tv;
+                int ti = sid[a]; sid[a] = sid[b]; sid[b] = ti;
+            }
+        }
+    }
+    // solver.cpp:270-296
+    double ph[3] = {0., 0., 0.};
+    double sum = 0.;
+    int oid[6];
+    double ov[6];
+#pragma unroll
+    for (int a = 0; a < PF_NSLOT64; a++) {
+        if (del[a] > cutoff) {
+            oid[a] = sid[a];
+            ov[a] = del[a];
+            const int p = pf_phase_of_grain(sid[a]);
+            if (p == 1) ph[0] += del[a];
+            else if (p == 2) ph[1] += del[a];
+            else if (p == 3) ph[2] += del[a];
+            sum += del[a];
+        } else {
+            oid[a] = 0;
+            ov[a] = 0.;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < PF_NSLOT64; a++) ov[a] *= 1. / sum;
+#pragma unroll
+    for (int p = 0; p < 3; p++) ph[p] *= 1. / sum;
+    {
+        int2 *op = reinterpret_cast<int2 *>(ids2 + 6 * n);
+        double2 *vp = reinterpret_cast<double2 *>(phi2 + 6 * n);
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            op[a] = make_int2(oid[2 * a], oid[2 * a + 1]);
+            vp[a] = make_double2(ov[2 * a], ov[2 * a + 1]);
+        }
+    }
+    phase[3 * n + 0] = ph[0];
+    phase[3 * n + 1] = ph[1];
+    phase[3 * n + 2] = ph[2];
+    // solver.cpp:299: partition in place, every solute.
+    for (int q = 0; q < P.nsol; q++) {
+        double out[3];
+        pf_partition(C[q * P.N + n], ph, P.k[q], P.c[q], out);
+        double *cp = conc1 + (long long)q * 3 * P.N + 3 * n;
+        cp[0] = out[0]; cp[1] = out[1]; cp[2] = out[2];
+    }
+}
+
+// Diffusion_solver (solver.cpp:343-372) for every solute, one thread per cell:
+// reads phase/conc1 of the cell and its nnb neighbours, updates C in place and
+// writes the re-partitioned concentrations to conc2.  With nnb = 6 and
+// coef = dt/num_loop/dx^2 it is also one sub-step of the reference's GPU
+// plug-in (gpu_solver.cpp:131-188): the partition written here is exactly what
+// GPU_Partitioning computes at the start of the next sub-step.
+__global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_step_params P, int nnb,
+                                                     double coef, const double *__restrict__ phase,
+                                                     const double *__restrict__ conc1,
+                                                     double *__restrict__ conc2,
+                                                     double *__restrict__ C) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    long long nbr[6];
+    pf_neighbours(n, P.ix, P.iy, P.iz, nbr);
+    double ph[3];
+    ph[0] = __ldg(phase + 3 * n + 0);
+    ph[1] = __ldg(phase + 3 * n + 1);
+    ph[2] = __ldg(phase + 3 * n + 2);
+    double nph[6][3];
+#pragma unroll
+    for (int b = 0; b < 6; b++)
+        if (b < nnb) {
+#pragma unroll
+            for (int p = 0; p < 3; p++) nph[b][p] = __ldg(phase + 3 * nbr[b] + p);
+        }
+    for (int q = 0; q < P.nsol; q++) {
+        const double *c1 = conc1 + (long long)q * 3 * P.N;
+        double cs[3];
+        cs[0] = __ldg(c1 + 3 * n + 0);
+        cs[1] = __ldg(c1 + 3 * n + 1);
+        cs[2] = __ldg(c1 + 3 * n + 2);
+        double del = 0.;
+#pragma unroll
+        for (int b = 0; b < 6; b++)
+            if (b < nnb) {
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+                    del += sqrt(nph[b][p] * ph[p]) * (__ldg(c1 + 3 * nbr[b] + p) - cs[p]) * P.D[q][p];
+            }
+        del *= coef;
+        const double cn = C[q * P.N + n] + del;
+        C[q * P.N + n] = cn;
+        double out[3];
+        pf_partition(cn, ph, P.k[q], P.c[q], out);
+        double *cp = conc2 + (long long)q * 3 * P.N + 3 * n;
+        cp[0] = out[0]; cp[1] = out[1]; cp[2] = out[2];
+    }
+}
+
+// Partitioning of every cell and solute (MicrostructureConstruction.cpp:53-62,
+// gpu_solver.cpp:131-154).
+__global__ void __launch_bounds__(256) k_partition_f64(const __grid_constant__ pf_step_params P,
+                                                       const double *__restrict__ phase,
+                                                       const double *__restrict__ C,
+                                                       double *__restrict__ conc) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    double ph[3] = {phase[3 * n], phase[3 * n + 1], phase[3 * n + 2]};
+    for (int q = 0; q < P.nsol; q++) {
+        double out[3];
+        pf_partition(C[q * P.N + n], ph, P.k[q], P.c[q], out);
+        double *cp = conc + (long long)q * 3 * P.N + 3 * n;
+        cp[0] = out[0]; cp[1] = out[1]; cp[2] = out[2];
+    }
+}
+
+inline unsigned pf_blocks(long long N, int threads) { return (unsigned)((N + threads - 1) / threads); }
+
+}  // namespace
+
+cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
+                                double *phi2, double *phase, double *conc1, const double *C,
+                                cudaStream_t s) {
+    k_phase_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C);
+    return cudaGetLastError();
+}
+
+cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
+                                  const double *conc1, double *conc2, double *C, cudaStream_t s) {
+    k_diffuse_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, nnb, coef, phase, conc1, conc2, C);
+    return cudaGetLastError();
+}
+
+cudaError_t pf_launch_partition_f64(const pf_step_params &P, const double *phase, const double *C,
+                                    double *conc, cudaStream_t s) {
+    k_partition_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, phase, C, conc);
+    return cudaGetLastError();
+}

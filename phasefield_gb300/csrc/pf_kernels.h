@@ -1,0 +1,49 @@
+// pf_kernels.h -- host-side launchers of the sm_103a kernels (internal to libpfstep).
+#pragma once
+#include <cuda_runtime.h>
+#include "pf_types.h"
+
+// ---- FP64 reference layout (pf_f64.cu) ----
+cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
+                                double *phi2, double *phase, double *conc1, const double *C,
+                                cudaStream_t s);
+cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
+                                  const double *conc1, double *conc2, double *C, cudaStream_t s);
+cudaError_t pf_launch_partition_f64(const pf_step_params &P, const double *phase, const double *C,
+                                    double *conc, cudaStream_t s);
+
+// ---- compact FP32 layout (pf_f32.cu) ----
+// gid: ushort4 per cell (local grain ids, 0 = empty), phi: float4 per cell,
+// phase: three float planes [3][N], sol: float2 (value, Kahan compensation)
+// per cell and solute, interleaved [N][nsol].
+struct pf_f32_map {
+    int off[4];    // local id offsets of grain classes 0..3 (id/100000)
+    int total;     // largest local id
+};
+cudaError_t pf_launch_id_span(const int *ids64, long long N, int *span4, cudaStream_t s);
+cudaError_t pf_launch_pack_f32(long long N, int nsol, const pf_f32_map &map, const int *ids64,
+                               const double *phi64, const double *phase64, const double *C64,
+                               ushort4 *gid, float4 *phi, float *phase, float2 *sol,
+                               unsigned int *n_truncated, cudaStream_t s);
+cudaError_t pf_launch_unpack_f32(const pf_step_params &P, const pf_f32_map &map, const ushort4 *gid,
+                                 const float4 *phi, const float *phase, const float2 *sol, int *ids64,
+                                 double *phi64, double *phase64, double *conc64, double *C64,
+                                 cudaStream_t s);
+cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, const float4 *phi1,
+                                ushort4 *gid2, float4 *phi2, float *phase, const float2 *sol,
+                                cudaStream_t s);
+cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *phase, const float2 *sol_in,
+                                  float2 *sol_out, cudaStream_t s);
+
+// ---- FP64 reductions (pf_reduce.cu) ----
+// out[0..2]  sum of phase fractions, out[3] sum of phi over slots whose grain
+// id is below 100000 (write_data.cpp:18), out[4..5] solute sums, out[6]
+// number of non-finite values seen.  'partials' holds 8 doubles per block.
+#define PF_RED_NOUT 8
+int pf_reduce_blocks(long long N);
+cudaError_t pf_launch_reduce_f64(long long N, int nsol, const int *ids, const double *phi,
+                                 const double *phase, const double *C, double *partials, int nblocks,
+                                 double *out, cudaStream_t s);
+cudaError_t pf_launch_reduce_f32(long long N, int nsol, int deformed_max_local, const ushort4 *gid,
+                                 const float4 *phi, const float *phase, const float2 *sol,
+                                 double *partials, int nblocks, double *out, cudaStream_t s);

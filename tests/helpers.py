@@ -1,0 +1,47 @@
+"""Shared helpers for the tests: small workloads built from the packaged
+configs, and comparisons between the product's GPU state and the oracle's."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+import phasefield_gb300 as pf
+import pyoracle as po
+from phasefield_gb300 import workloads as W
+
+
+def small_case(tmpdir: str, name: str, grid, *, T=None, n_grains=None, n_nuclei=None, radius=None,
+               n_particles=None, noise=None, seed=0, max_slots=4, mn=True):
+    """A reduced copy of a packaged workload: returns (pf_model, oracle_model, spec)."""
+    wl = W.WORKLOADS[name]
+    os.makedirs(tmpdir, exist_ok=True)
+    W.write_thermo(os.path.join(tmpdir, "thermo_steel.txt"))
+    cfg = W.write_config(os.path.join(tmpdir, f"{name}_small.txt"), grid=grid, dx=wl.dx,
+                         T=wl.T if T is None else T, mn=mn, directory=os.path.join(tmpdir, "out"))
+    m = pf.read_model(cfg)
+    om = po.load_model(cfg)
+    spec = wl.spec()
+    if n_grains is not None:
+        spec.n_grains = n_grains
+    if n_nuclei is not None:
+        spec.n_nuclei = n_nuclei
+    if radius is not None:
+        spec.nucleus_radius = radius
+    if n_particles is not None:
+        spec.n_particles = n_particles
+    if noise is not None:
+        spec.C_noise[0], spec.C_noise[1] = noise
+    spec.seed = seed
+    spec.max_slots = max_slots
+    return m, om, spec
+
+
+def copy_state(st: dict) -> dict:
+    return {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in st.items()}
+
+
+def rel_maxnorm(a: np.ndarray, b: np.ndarray) -> float:
+    """max|a-b| / max(max|b|, tiny): the relative max-norm used for parity."""
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(a - b))) / scale
