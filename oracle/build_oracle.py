@@ -49,6 +49,22 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
+RUNNER = os.path.join(BUILD, "libref_runner.so")
+
+
+def build_ref_runner(force: bool = False) -> str:
+    """Driver-API host loop that launches the reference's kernels from a cubin."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "ref_runner.cpp")
+    if force or _newer(RUNNER, [src, __file__]):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", src, "-o", RUNNER,
+               "-I", os.path.join(CUDA_HOME, "include"), "-L", os.path.join(CUDA_HOME, "lib64", "stubs"), "-lcuda"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference runner build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+    return RUNNER
+
+
 def build_ref(force: bool = False) -> list[str]:
     """Compile the reference's GPU plug-in kernels (where the checkout exists)."""
     src = os.path.join(REF_SRC, "gpu_solver.cpp")

@@ -295,6 +295,40 @@ def fractions(m: OModel, ids, phi, phase) -> np.ndarray:
     return out
 
 
+RUNNER_PATH = os.path.join(HERE, "_build", "libref_runner.so")
+REF_CUBINS = {"fma": os.path.join(HERE, "_ref", "gpu_solver_ref.cubin"),
+              "nofma": os.path.join(HERE, "_ref", "gpu_solver_ref_nofma.cubin")}
+_runner = None
+
+
+def ref_kernels_available() -> bool:
+    return all(os.path.exists(p) for p in REF_CUBINS.values())
+
+
+def ref_gpu_diffusion_solver(variant, D3, k9, c9, phase, C, x, y, z, dt, dx) -> int:
+    """Run the reference's own GPU_Partitioning/Diff3D kernels (cubin built from
+    gpu_solver.cpp) under the host loop of GPU_Diffusion_solver; C in place."""
+    global _runner
+    if _runner is None:
+        import build_oracle
+
+        build_oracle.build_ref_runner()
+        R = ctypes.CDLL(RUNNER_PATH)
+        R.ref_gpu_diffusion_solver.argtypes = [ctypes.c_char_p, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, _D, _D]
+        R.ref_gpu_diffusion_solver.restype = ctypes.c_int
+        R.ref_last_error.restype = ctypes.c_char_p
+        _runner = R
+    D3 = np.ascontiguousarray(D3, np.float64)
+    k9 = np.ascontiguousarray(k9, np.float64)
+    c9 = np.ascontiguousarray(c9, np.float64)
+    n = _runner.ref_gpu_diffusion_solver(REF_CUBINS[variant].encode(), _ptr(D3), _ptr(k9), _ptr(c9), _ptr(phase),
+                                         _ptr(C), x, y, z, dt, dx)
+    if n < 0:
+        raise RuntimeError("reference kernels: " + _runner.ref_last_error().decode())
+    return n
+
+
 def set_threads(n: int) -> None:
     lib().pfo_set_num_threads(n)
 

@@ -12,7 +12,7 @@ from phasefield_gb300 import workloads as W
 
 
 def small_case(tmpdir: str, name: str, grid, *, T=None, n_grains=None, n_nuclei=None, radius=None,
-               n_particles=None, noise=None, seed=0, max_slots=4, mn=True):
+               n_particles=None, noise=None, seed=0, max_slots=4, mn=True, C0=None):
     """A reduced copy of a packaged workload: returns (pf_model, oracle_model, spec)."""
     wl = W.WORKLOADS[name]
     os.makedirs(tmpdir, exist_ok=True)
@@ -32,6 +32,8 @@ def small_case(tmpdir: str, name: str, grid, *, T=None, n_grains=None, n_nuclei=
         spec.n_particles = n_particles
     if noise is not None:
         spec.C_noise[0], spec.C_noise[1] = noise
+    if C0 is not None:
+        spec.C0[0], spec.C0[1] = C0
     spec.seed = seed
     spec.max_slots = max_slots
     return m, om, spec
