@@ -198,7 +198,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     N = wl.N
     P = pf.params_at(m, 0.0)
     nsol = m.nsol
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: every context launches on it and the CUDA events are
+    # recorded on it (torch's default stream has handle 0, which the C ABI
+    # reads as "use the context's own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
 
     def barrier():
         if world > 1:
