@@ -200,6 +200,21 @@ int pf_write_data(pf_ctx *ctx, const char *directory, int forced, int *written);
 int pf_write_vti(const char *path, int ix, int iy, int iz, double dx, const int32_t *ids,
                  const double *C);
 
+/* No counterpart in the reference.  The statistics of pf_reduce (same 8
+ * outputs, written to the device array d_out) for caller-owned device arrays in
+ * the reference layout, computed without allocating anything: for callers that
+ * cannot call cudaMalloc -- an application pool that owns all device memory, a
+ * framework caching allocator, or a loop that cannot take cudaMalloc's implicit
+ * device synchronisation.  The scratch is a fixed 256 KiB __device__ array
+ * held by every GPU that loads the library; N is limited to
+ * PF_NOALLOC_MAX_CELLS (PF_ERR_RANGE beyond it).  The first call on a device
+ * looks up the array's device address and should come before any stream
+ * capture.  Asynchronous on cuda_stream (NULL = the legacy default stream);
+ * calls that overlap on the GPU share the array and race. */
+#define PF_NOALLOC_MAX_CELLS 16777216LL
+int pf_reduce_noalloc(long long N, int nsol, const int32_t *d_ids, const double *d_phi,
+                      const double *d_phase, const double *d_C, double *d_out, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -136,6 +136,7 @@ SYMBOLS = {
     "pf_use_graph": (_I, [_P, _I]),
     "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
     "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
+    "pf_reduce_noalloc": (_I, [ctypes.c_longlong, _I, _P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

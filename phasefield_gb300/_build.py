@@ -49,7 +49,7 @@ PER_FILE = {
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
              "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_reduce.cu", "pf_api.cu"]
+CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_reduce.cu", "pf_api.cu", "pf_reduce_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
 HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_kernels.h", "pf_host.h"]
 
