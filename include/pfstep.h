@@ -178,6 +178,9 @@ int pf_download_state(pf_ctx *ctx, int32_t *ids, double *phi, double *phase, dou
                       double *time);
 /* Advance nsteps full time steps (asynchronous on the context's stream). */
 int pf_step(pf_ctx *ctx, int nsteps);
+/* Only the diffusion sub-cycle: nsub sub-steps with the parameters of the
+ * current time, phases fixed, time not advanced (phase_field.cpp:408-418 alone). */
+int pf_diffuse(pf_ctx *ctx, int nsub);
 /* FP64 statistics: out[0..2] sum of phase fractions over cells, out[3] sum of
  * phi over slots with grain id < 100000, out[4..5] solute totals, out[6] 0,
  * out[7] count of non-finite values.  Divide by N for write_data.cpp:14-18. */

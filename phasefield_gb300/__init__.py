@@ -126,6 +126,7 @@ SYMBOLS = {
     "pf_upload_state": (_I, [_P, _P, _P, _P, _P, _P, _D]),
     "pf_download_state": (_I, [_P, _P, _P, _P, _P, _P, _DP]),
     "pf_step": (_I, [_P, _I]),
+    "pf_diffuse": (_I, [_P, _I]),
     "pf_reduce": (_I, [_P, _DP]),
     "pf_synchronize": (_I, [_P]),
     "pf_get_time": (_I, [_P, _DP]),
@@ -250,6 +251,10 @@ class PhaseField:
     def update(self, nsteps: int = 1) -> None:
         """phase_field::Update(false) nsteps times (phase_field.cpp:243-305)."""
         check(lib().pf_step(self._ctx, nsteps), "pf_step")
+
+    def diffuse(self, nsub: int) -> None:
+        """Only the diffusion sub-cycle (phases fixed, time not advanced)."""
+        check(lib().pf_diffuse(self._ctx, nsub), "pf_diffuse")
 
     def synchronize(self) -> None:
         check(lib().pf_synchronize(self._ctx), "pf_synchronize")

@@ -522,6 +522,33 @@ extern "C" int pf_step(pf_ctx *c, int nsteps) {
     return PF_OK;
 }
 
+extern "C" int pf_diffuse(pf_ctx *c, int nsub) {
+    if (!c || !c->have_state) return pf_fail(PF_ERR_ARG, "pf_diffuse: no state uploaded");
+    if (nsub < 0) return pf_fail(PF_ERR_ARG, "pf_diffuse: negative sub-step count");
+    pf_step_params P;
+    pf_compute_params(c->model, c->time, P);
+    cudaError_t e = cudaSuccess;
+    if (c->prec == PF_PREC_FP64) {
+        for (int it = 0; it < nsub && e == cudaSuccess; it++) {
+            const int b = c->curc;
+            e = timed(c, 1, [&] {
+                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->phase, c->conc[b], c->conc[1 - b], c->C,
+                                             c->stream);
+            });
+            c->curc = 1 - b;
+        }
+    } else {
+        pf_f32_params F;
+        pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
+        for (int it = 0; it < nsub && e == cudaSuccess; it++) {
+            const int b = c->curs;
+            e = timed(c, 1, [&] { return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream); });
+            c->curs = 1 - b;
+        }
+    }
+    return e == cudaSuccess ? PF_OK : pf_cuda_fail(e);
+}
+
 extern "C" int pf_reduce(pf_ctx *c, double out[8]) {
     if (!c || !c->have_state || !out) return pf_fail(PF_ERR_ARG, "pf_reduce: no state");
     cudaError_t e;

@@ -197,54 +197,168 @@ __global__ void __launch_bounds__(256) k_phase_f32(const __grid_constant__ pf_f3
     phase[2 * P.N + n] = ph[2] * inv;
 }
 
-// One diffusion sub-step (solver.cpp:343-372) for all solutes: flux from the
-// re-partitioned phase concentrations of the cell and its neighbours, then a
-// Kahan-compensated update of the solute total.  D already carries dt_sub/dx^2.
+// ---------------------------------------------------------------------------
+// One diffusion sub-step (solver.cpp:343-372) for all solutes.
+//
+// Every cell contributes two derived quantities to its neighbours' fluxes:
+// s_p = sqrt(phi_p) (the flux weight sqrt(phi_p^nb phi_p) = s_p^nb s_p) and the
+// partitioned phase concentrations c_p (solver.cpp:389-405).  They are computed
+// once per cell: a block owns a TX x TY tile of the x-y plane and marches up a
+// chunk of z planes.  The derived values of the current plane, with a one-cell
+// in-plane halo, sit in shared memory; those of the planes below and above the
+// thread's own column sit in registers.  Each thread then loads its cell's raw
+// data once (phase fractions + solute totals), halo cells are re-read from L2.
+// The solute total is advanced with a Kahan-compensated sum; D already
+// carries dt_sub/dx^2.
+// ---------------------------------------------------------------------------
 template <int NSOL>
-__global__ void __launch_bounds__(256) k_diffuse_f32(const __grid_constant__ pf_f32_params P,
-                                                     const float *__restrict__ phase,
-                                                     const float2 *__restrict__ sol_in,
-                                                     float2 *__restrict__ sol_out) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
-    long long nbr[6];
-    pf_neighbours(n, P.ix, P.iy, P.iz, nbr);
-    const long long N = P.N;
-    float ph[3] = {__ldg(phase + n), __ldg(phase + N + n), __ldg(phase + 2 * N + n)};
-    float sq[3] = {sqrtf(ph[0]), sqrtf(ph[1]), sqrtf(ph[2])};
-    float2 so[NSOL];
-    float cs[NSOL][3];
-#pragma unroll
-    for (int q = 0; q < NSOL; q++) {
-        so[q] = __ldg(sol_in + n * NSOL + q);
-        pf_partition_f32(so[q].x, ph, P.k[q], P.c[q], cs[q]);
+struct pf_der {
+    float s[3];
+    float c[NSOL][3];
+};
+
+template <int NSOL>
+__device__ __forceinline__ void pf_load_raw(const float *__restrict__ phase, const float2 *__restrict__ sol,
+                                            long long N, long long n, float ph[3], float2 so[NSOL]) {
+    ph[0] = __ldg(phase + n);
+    ph[1] = __ldg(phase + N + n);
+    ph[2] = __ldg(phase + 2 * N + n);
+    if (NSOL == 2) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(sol) + n);
+        so[0] = make_float2(v.x, v.y);
+        so[NSOL - 1] = make_float2(v.z, v.w);
+    } else {
+        so[0] = __ldg(sol + n);
     }
-    float flux[NSOL];
+}
+
+template <int NSOL>
+__device__ __forceinline__ void pf_derive(const pf_f32_params &P, const float ph[3], const float2 so[NSOL],
+                                          pf_der<NSOL> &d) {
 #pragma unroll
-    for (int q = 0; q < NSOL; q++) flux[q] = 0.f;
+    for (int p = 0; p < 3; p++) d.s[p] = sqrtf(ph[p]);
 #pragma unroll
-    for (int b = 0; b < 6; b++) {
-        if (b < P.nnb) {
-            const long long m = nbr[b];
-            float nph[3] = {__ldg(phase + m), __ldg(phase + N + m), __ldg(phase + 2 * N + m)};
-            float w[3];
+    for (int q = 0; q < NSOL; q++) pf_partition_f32(so[q].x, ph, P.k[q], P.c[q], d.c[q]);
+}
+
+__device__ __forceinline__ int pf_mod(int v, int L) {
+    v %= L;
+    return v < 0 ? v + L : v;
+}
+
+template <int NSOL, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY) k_diffuse_f32(const __grid_constant__ pf_f32_params P,
+                                                        const float *__restrict__ phase,
+                                                        const float2 *__restrict__ sol_in,
+                                                        float2 *__restrict__ sol_out, int zchunk) {
+    constexpr int W = TX + 2, H = TY + 2;
+    static_assert(2 * TX + 2 * TY <= TX * TY, "halo needs one thread per halo cell");
+    __shared__ float sm_s[3][H][W];
+    __shared__ float sm_c[NSOL][3][H][W];
+    const int ix = P.ix, iy = P.iy, iz = P.iz;
+    const long long N = P.N;
+    const long long plane = (long long)ix * iy;
+    const int tiles_x = (ix + TX - 1) / TX;
+    const int tx0 = (int)(blockIdx.x % tiles_x) * TX;
+    const int ty0 = (int)(blockIdx.x / tiles_x) * TY;
+    const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+    const bool valid = (tx0 + lx < ix) && (ty0 + ly < iy);
+    // Every shared slot holds the cell at the wrapped coordinates, so partial
+    // tiles and periodic neighbours need no special case.
+    const long long col = pf_mod(tx0 + lx, ix) + (long long)ix * pf_mod(ty0 + ly, iy);
+    constexpr int NHALO = 2 * TX + 2 * TY;
+    const bool has_halo = threadIdx.x < NHALO;
+    int hx = 0, hy = 0;
+    {
+        const int h = threadIdx.x;
+        if (h < TX) { hx = h; hy = -1; }
+        else if (h < 2 * TX) { hx = h - TX; hy = TY; }
+        else if (h < 2 * TX + TY) { hx = -1; hy = h - 2 * TX; }
+        else { hx = TX; hy = h - 2 * TX - TY; }
+    }
+    const long long hcol = pf_mod(tx0 + hx, ix) + (long long)ix * pf_mod(ty0 + hy, iy);
+    const bool use_y = P.nnb >= 4, use_z = P.nnb >= 6;
+    const int z0 = blockIdx.y * zchunk;
+    const int z1 = min(z0 + zchunk, iz);
+
+    pf_der<NSOL> dprev, dcur, dnext;
+    float2 so_cur[NSOL], so_nxt[NSOL];
+    {
+        float ph[3];
+        if (use_z) {
+            pf_load_raw<NSOL>(phase, sol_in, N, col + plane * pf_mod(z0 - 1, iz), ph, so_nxt);
+            pf_derive<NSOL>(P, ph, so_nxt, dprev);
+        }
+        pf_load_raw<NSOL>(phase, sol_in, N, col + plane * z0, ph, so_cur);
+        pf_derive<NSOL>(P, ph, so_cur, dcur);
+    }
+    for (int z = z0; z < z1; z++) {
+        // Issue this plane's halo loads and the next plane's own loads first.
+        float hph[3] = {0.f, 0.f, 0.f};
+        float2 hso[NSOL];
+        if (has_halo) pf_load_raw<NSOL>(phase, sol_in, N, hcol + plane * z, hph, hso);
+        const bool need_next = use_z || (z + 1 < z1);
+        float nph[3] = {0.f, 0.f, 0.f};
+        if (need_next) pf_load_raw<NSOL>(phase, sol_in, N, col + plane * pf_mod(z + 1, iz), nph, so_nxt);
 #pragma unroll
-            for (int p = 0; p < 3; p++) w[p] = sqrtf(nph[p]) * sq[p];
+        for (int p = 0; p < 3; p++) {
+            sm_s[p][ly + 1][lx + 1] = dcur.s[p];
 #pragma unroll
-            for (int q = 0; q < NSOL; q++) {
-                float cn[3];
-                pf_partition_f32(__ldg(sol_in + m * NSOL + q).x, nph, P.k[q], P.c[q], cn);
+            for (int q = 0; q < NSOL; q++) sm_c[q][p][ly + 1][lx + 1] = dcur.c[q][p];
+        }
+        if (has_halo) {
+            pf_der<NSOL> dh;
+            pf_derive<NSOL>(P, hph, hso, dh);
 #pragma unroll
-                for (int p = 0; p < 3; p++) flux[q] += w[p] * (cn[p] - cs[q][p]) * P.D[q][p];
+            for (int p = 0; p < 3; p++) {
+                sm_s[p][hy + 1][hx + 1] = dh.s[p];
+#pragma unroll
+                for (int q = 0; q < NSOL; q++) sm_c[q][p][hy + 1][hx + 1] = dh.c[q][p];
             }
         }
-    }
+        __syncthreads();
+        if (need_next) pf_derive<NSOL>(P, nph, so_nxt, dnext);
+        float acc[NSOL][3];
 #pragma unroll
-    for (int q = 0; q < NSOL; q++) {
-        const float y = flux[q] - so[q].y;
-        const float t = so[q].x + y;
-        const float comp = (t - so[q].x) - y;
-        sol_out[n * NSOL + q] = make_float2(t, comp);
+        for (int p = 0; p < 3; p++) {
+#pragma unroll
+            for (int q = 0; q < NSOL; q++) {
+                const float c0 = dcur.c[q][p];
+                float a = sm_s[p][ly + 1][lx] * (sm_c[q][p][ly + 1][lx] - c0);
+                a += sm_s[p][ly + 1][lx + 2] * (sm_c[q][p][ly + 1][lx + 2] - c0);
+                if (use_y) {
+                    a += sm_s[p][ly][lx + 1] * (sm_c[q][p][ly][lx + 1] - c0);
+                    a += sm_s[p][ly + 2][lx + 1] * (sm_c[q][p][ly + 2][lx + 1] - c0);
+                }
+                if (use_z) {
+                    a += dprev.s[p] * (dprev.c[q][p] - c0);
+                    a += dnext.s[p] * (dnext.c[q][p] - c0);
+                }
+                acc[q][p] = a;
+            }
+        }
+        if (valid) {
+            const long long n = col + plane * z;
+#pragma unroll
+            for (int q = 0; q < NSOL; q++) {
+                const float flux = dcur.s[0] * P.D[q][0] * acc[q][0] + dcur.s[1] * P.D[q][1] * acc[q][1] +
+                                   dcur.s[2] * P.D[q][2] * acc[q][2];
+                const float y = flux - so_cur[q].y;
+                const float t = so_cur[q].x + y;
+                const float comp = (t - so_cur[q].x) - y;
+                so_cur[q] = make_float2(t, comp);
+            }
+            if (NSOL == 2)
+                reinterpret_cast<float4 *>(sol_out)[n] =
+                    make_float4(so_cur[0].x, so_cur[0].y, so_cur[NSOL - 1].x, so_cur[NSOL - 1].y);
+            else
+                sol_out[n] = so_cur[0];
+        }
+        __syncthreads();
+        dprev = dcur;
+        dcur = dnext;
+#pragma unroll
+        for (int q = 0; q < NSOL; q++) so_cur[q] = so_nxt[q];
     }
 }
 
@@ -447,9 +561,16 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
 
 cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *phase, const float2 *sol_in,
                                   float2 *sol_out, cudaStream_t s) {
+    constexpr int TX = 32, TY = 8;
+    const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
+    // z chunk: enough blocks for several waves on 152 SMs, at least 8 planes
+    // per block to amortise the two extra planes of the prologue.
+    int zchunk = P.iz;
+    while (zchunk > 8 && (long long)tiles * ((P.iz + zchunk - 1) / zchunk) < 152 * 16) zchunk = (zchunk + 1) / 2;
+    const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
     if (P.nsol == 2)
-        k_diffuse_f32<2><<<pf_blocks(P.N, 256), 256, 0, s>>>(P, phase, sol_in, sol_out);
+        k_diffuse_f32<2, TX, TY><<<grid, TX * TY, 0, s>>>(P, phase, sol_in, sol_out, zchunk);
     else
-        k_diffuse_f32<1><<<pf_blocks(P.N, 256), 256, 0, s>>>(P, phase, sol_in, sol_out);
+        k_diffuse_f32<1, TX, TY><<<grid, TX * TY, 0, s>>>(P, phase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
 }
