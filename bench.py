@@ -28,6 +28,7 @@ value = all ranks' cells x steps / max-over-ranks time ("scaling": "weak").
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -191,11 +192,12 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     torch.cuda.set_device(local_rank)
     dev = torch.cuda.current_device()
     wl = _workload(args.workload)
-    cfg, m = _model_for(wl)
-    spec = wl.spec()
+    grid = tuple(args.grid) if args.grid else wl.grid
+    cfg, m = _model_for(wl, grid)
+    spec = _scaled_spec(wl, grid) if args.grid else wl.spec()
     spec.seed = wl.seed + rank
     st0 = pf.init_microstructure(m, spec, 0.0)
-    N = wl.N
+    N = grid[0] * grid[1] * grid[2]
     P = pf.params_at(m, 0.0)
     nsol = m.nsol
     # A dedicated stream: every context launches on it and the CUDA events are
@@ -238,41 +240,40 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     F.enable_kernel_timing(False)
     F.close()
 
-    pk = _peaks()
-    diff_bytes = N * (12 + 16 * nsol)           # algorithmic bytes per diffusion sub-step
-    phase_bytes = N * (60 + 8 * nsol)           # algorithmic bytes per phase sweep
-    t_diff = kt["diffusion"][0] / max(1, kt["diffusion"][1]) / 1e3
-    t_phase = kt["phase"][0] / max(1, kt["phase"][1]) / 1e3
-    ach = diff_bytes / t_diff / 1e9
-    step_bytes = phase_bytes + P.n_sub * diff_bytes
-
     # ---- FP64 plain step on the same workload ----------------------------
-    k64 = max(1, min(args.steps, args.fp64_steps))
-    G = pf.PhaseField(m, pf.PF_PREC_FP64)
-    G.set_stream(stream.cuda_stream)
-    G.upload(st0, 0.0)
-    G.update(1)
-    G.enable_kernel_timing(True)
-    torch.cuda.synchronize()
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record(stream)
-    G.update(k64)
-    g1.record(stream)
-    torch.cuda.synchronize()
-    ms64 = max_over_ranks(g0.elapsed_time(g1))
-    kt64 = G.kernel_times()
-    G.close()
-    value64 = world * N * k64 / (ms64 / 1e3)
+    fp64 = None
+    if args.fp64_steps > 0:
+        k64 = max(1, min(args.steps, args.fp64_steps))
+        G = pf.PhaseField(m, pf.PF_PREC_FP64)
+        G.set_stream(stream.cuda_stream)
+        G.upload(st0, 0.0)
+        G.update(1)
+        G.enable_kernel_timing(True)
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        G.update(k64)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = max_over_ranks(g0.elapsed_time(g1))
+        kt64 = G.kernel_times()
+        G.close()
+        value64 = world * N * k64 / (ms64 / 1e3)
+        fp64 = {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
+                "phase_ms": kt64["phase"][0] / max(1, kt64["phase"][1]),
+                "diffusion_ms": kt64["diffusion"][0] / max(1, kt64["diffusion"][1])}
+    if args.no_e2e:
+        return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk)
 
     # ---- e2e: through the C ABI with pinned host buffers -----------------
     keep_alive = []
 
-    def pinned(a: np.ndarray) -> np.ndarray:
-        t = torch.empty(a.size, dtype={np.int32: torch.int32, np.float64: torch.float64}[a.dtype.type],
+    def pinned(arr: np.ndarray) -> np.ndarray:
+        t = torch.empty(arr.size, dtype={np.int32: torch.int32, np.float64: torch.float64}[arr.dtype.type],
                         pin_memory=True)
         keep_alive.append(t)
         out = t.numpy()
-        out[:] = a
+        out[:] = arr
         return out
 
     host = {k: pinned(v) for k, v in st0.items()}
@@ -288,11 +289,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     for _ in range(args.steps):
         H.update(1)
         H.fractions()  # device -> host read of the step's statistics (64 bytes)
-    import ctypes
-    L = pf.lib()
     tt = ctypes.c_double()
-    pf.check(L.pf_download_state(H._ctx, pf._ptr(back["ids"]), pf._ptr(back["phi"]), pf._ptr(back["phase"]),
-                                 pf._ptr(back["conc"]), pf._ptr(back["C"]), ctypes.byref(tt)), "download")
+    pf.check(pf.lib().pf_download_state(H._ctx, pf._ptr(back["ids"]), pf._ptr(back["phi"]), pf._ptr(back["phase"]),
+                                        pf._ptr(back["conc"]), pf._ptr(back["C"]), ctypes.byref(tt)), "download")
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     H.close()
     state_bytes = sum(int(v.nbytes) for k, v in st0.items() if k in ("ids", "phi", "phase", "C"))
@@ -300,9 +299,19 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     e2e = {"value": world * N * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(state_bytes / args.steps),
            "d2h_bytes_per_step": int(64 + down_bytes / args.steps)}
+    return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk)
 
+
+def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk):
     if rank != 0:
         return None
+    pk = _peaks()
+    diff_bytes = N * (12 + 16 * nsol)           # algorithmic bytes per diffusion sub-step
+    phase_bytes = N * (60 + 8 * nsol)           # algorithmic bytes per phase sweep
+    t_diff = kt["diffusion"][0] / max(1, kt["diffusion"][1]) / 1e3
+    t_phase = kt["phase"][0] / max(1, kt["phase"][1]) / 1e3
+    ach = diff_bytes / t_diff / 1e9
+    step_bytes = phase_bytes + P.n_sub * diff_bytes
 
     # ---- CPU baseline (oracle, bounded sample) ----------------------------
     cpu = None
@@ -325,10 +334,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 (Kahan-compensated solutes, fp64 reductions)",
         "data": "synthetic (seeded Voronoi grains + nuclei, uniform noise)",
-        "config": {"workload": f"{wl.name}: {wl.grid[0]}x{wl.grid[1]}x{wl.grid[2]} cells, {wl.n_grains} grains, "
+        "config": {"workload": f"{wl.name}: {grid[0]}x{grid[1]}x{grid[2]} cells, {wl.n_grains} grains, "
                                f"{wl.n_nuclei} nuclei r={wl.nucleus_radius}, C/Mn {wl.C0} +-{wl.C_noise[0]} wt%, "
                                f"T={wl.T} K, n_sub={P.n_sub}",
-                   "grid": list(wl.grid), "n_sub": P.n_sub, "solutes": nsol,
+                   "grid": list(grid), "n_sub": P.n_sub, "solutes": nsol,
                    "l2": f"inputs larger than L2 (FP32 state {N * 52 / 1e9:.2f} GB, L2 0.13 GB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -342,10 +351,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                               "bytes_per_launch": diff_bytes},
             "step_gbs_effective": step_bytes * args.steps / (ms / 1e3) / 1e9,
         },
-        "fp64": {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
-                 "phase_ms": kt64["phase"][0] / max(1, kt64["phase"][1]),
-                 "diffusion_ms": kt64["diffusion"][0] / max(1, kt64["diffusion"][1])},
-        "fp32_over_fp64": value / value64,
+        "fp64": fp64,
+        "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
         "fractions_end": [float(x) for x in fr_end[:3]],
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -363,6 +370,8 @@ def main() -> None:
     ap.add_argument("--workload", default="3d256")
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

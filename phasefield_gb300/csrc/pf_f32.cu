@@ -246,89 +246,179 @@ __device__ __forceinline__ int pf_mod(int v, int L) {
     return v < 0 ? v + L : v;
 }
 
+// Asynchronous global -> shared copies (cp.async): raw plane data is staged two
+// planes ahead so its latency overlaps the flux computation.  Each thread only
+// ever reads back what it copied itself, so the stages need no barrier.
+__device__ __forceinline__ void pf_cp_async4(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void pf_cp_async8(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void pf_cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void pf_cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void pf_cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+template <int NSOL>
+struct pf_solvec;
+template <>
+struct pf_solvec<1> { using T = float2; };
+template <>
+struct pf_solvec<2> { using T = float4; };
+
+template <int NSOL, int TX, int TY, int NST>
+struct pf_diff_smem {
+    using SV = typename pf_solvec<NSOL>::T;
+    static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2;
+    SV so[NST][NT];          // raw solute totals, own cells
+    SV hso[NST][NH];         // raw solute totals, halo cells
+    float ph[NST][3][NT];    // raw phase fractions, own cells
+    float hph[NST][3][NH];   // raw phase fractions, halo cells
+    float ds[3][H][W];       // derived sqrt(phi_p), current plane with halo
+    float dc[NSOL][3][H][W]; // derived phase concentrations, current plane with halo
+};
+
+template <int NSOL>
+__device__ __forceinline__ void pf_unpack_sol(const typename pf_solvec<NSOL>::T &v, float2 so[NSOL]);
+template <>
+__device__ __forceinline__ void pf_unpack_sol<1>(const float2 &v, float2 so[1]) { so[0] = v; }
+template <>
+__device__ __forceinline__ void pf_unpack_sol<2>(const float4 &v, float2 so[2]) {
+    so[0] = make_float2(v.x, v.y);
+    so[1] = make_float2(v.z, v.w);
+}
+
 template <int NSOL, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY) k_diffuse_f32(const __grid_constant__ pf_f32_params P,
-                                                        const float *__restrict__ phase,
-                                                        const float2 *__restrict__ sol_in,
-                                                        float2 *__restrict__ sol_out, int zchunk) {
-    constexpr int W = TX + 2, H = TY + 2;
-    static_assert(2 * TX + 2 * TY <= TX * TY, "halo needs one thread per halo cell");
-    __shared__ float sm_s[3][H][W];
-    __shared__ float sm_c[NSOL][3][H][W];
+__global__ void __launch_bounds__(TX *TY, 4) k_diffuse_f32(const __grid_constant__ pf_f32_params P,
+                                                           const float *__restrict__ phase,
+                                                           const float2 *__restrict__ sol_in,
+                                                           float2 *__restrict__ sol_out, int zchunk) {
+    constexpr int NST = 3;
+    using SM = pf_diff_smem<NSOL, TX, TY, NST>;
+    using SV = typename pf_solvec<NSOL>::T;
+    static_assert(SM::NH <= SM::NT, "halo needs one thread per halo cell");
+    extern __shared__ __align__(16) unsigned char pf_smem_raw[];
+    SM &sm = *reinterpret_cast<SM *>(pf_smem_raw);
     const int ix = P.ix, iy = P.iy, iz = P.iz;
     const long long N = P.N;
     const long long plane = (long long)ix * iy;
     const int tiles_x = (ix + TX - 1) / TX;
     const int tx0 = (int)(blockIdx.x % tiles_x) * TX;
     const int ty0 = (int)(blockIdx.x / tiles_x) * TY;
-    const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+    const int tid = threadIdx.x;
+    const int lx = tid % TX, ly = tid / TX;
     const bool valid = (tx0 + lx < ix) && (ty0 + ly < iy);
     // Every shared slot holds the cell at the wrapped coordinates, so partial
     // tiles and periodic neighbours need no special case.
     const long long col = pf_mod(tx0 + lx, ix) + (long long)ix * pf_mod(ty0 + ly, iy);
-    constexpr int NHALO = 2 * TX + 2 * TY;
-    const bool has_halo = threadIdx.x < NHALO;
+    const bool has_halo = tid < SM::NH;
     int hx = 0, hy = 0;
-    {
-        const int h = threadIdx.x;
-        if (h < TX) { hx = h; hy = -1; }
-        else if (h < 2 * TX) { hx = h - TX; hy = TY; }
-        else if (h < 2 * TX + TY) { hx = -1; hy = h - 2 * TX; }
-        else { hx = TX; hy = h - 2 * TX - TY; }
-    }
+    if (tid < TX) { hx = tid; hy = -1; }
+    else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
+    else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
+    else { hx = TX; hy = tid - 2 * TX - TY; }
     const long long hcol = pf_mod(tx0 + hx, ix) + (long long)ix * pf_mod(ty0 + hy, iy);
     const bool use_y = P.nnb >= 4, use_z = P.nnb >= 6;
     const int z0 = blockIdx.y * zchunk;
     const int z1 = min(z0 + zchunk, iz);
+    // Planes this block reads: z0-1 .. z1 with z neighbours, z0 .. z1-1 without.
+    const int zlo = use_z ? z0 - 1 : z0, zhi = use_z ? z1 : z1 - 1;
+    const SV *solv = reinterpret_cast<const SV *>(sol_in);
+
+    auto issue = [&](int zz) {  // stage raw data of plane zz (if needed), always commit a group
+        if (zz >= zlo && zz <= zhi) {
+            const int st = (zz - zlo) % NST;
+            const long long pz = plane * pf_mod(zz, iz);
+            const long long n = col + pz;
+            pf_cp_async4(&sm.ph[st][0][tid], phase + n);
+            pf_cp_async4(&sm.ph[st][1][tid], phase + N + n);
+            pf_cp_async4(&sm.ph[st][2][tid], phase + 2 * N + n);
+            if (NSOL == 2) pf_cp_async16(&sm.so[st][tid], solv + n);
+            else pf_cp_async8(&sm.so[st][tid], solv + n);
+            if (has_halo && zz >= z0 && zz < z1) {
+                const long long h = hcol + pz;
+                pf_cp_async4(&sm.hph[st][0][tid], phase + h);
+                pf_cp_async4(&sm.hph[st][1][tid], phase + N + h);
+                pf_cp_async4(&sm.hph[st][2][tid], phase + 2 * N + h);
+                if (NSOL == 2) pf_cp_async16(&sm.hso[st][tid], solv + h);
+                else pf_cp_async8(&sm.hso[st][tid], solv + h);
+            }
+        }
+        pf_cp_commit();
+    };
+    auto own_raw = [&](int zz, float ph[3], float2 so[NSOL]) {
+        const int st = (zz - zlo) % NST;
+        ph[0] = sm.ph[st][0][tid];
+        ph[1] = sm.ph[st][1][tid];
+        ph[2] = sm.ph[st][2][tid];
+        pf_unpack_sol<NSOL>(sm.so[st][tid], so);
+    };
 
     pf_der<NSOL> dprev, dcur, dnext;
-    float2 so_cur[NSOL], so_nxt[NSOL];
+    float2 so_cur[NSOL];
+    issue(zlo);
+    issue(zlo + 1);
+    if (use_z) issue(zlo + 2);
+    pf_cp_wait1();  // planes zlo and zlo+1 have landed (each thread's own copies)
     {
         float ph[3];
+        float2 so[NSOL];
         if (use_z) {
-            pf_load_raw<NSOL>(phase, sol_in, N, col + plane * pf_mod(z0 - 1, iz), ph, so_nxt);
-            pf_derive<NSOL>(P, ph, so_nxt, dprev);
+            own_raw(z0 - 1, ph, so);
+            pf_derive<NSOL>(P, ph, so, dprev);
         }
-        pf_load_raw<NSOL>(phase, sol_in, N, col + plane * z0, ph, so_cur);
+        own_raw(z0, ph, so_cur);
         pf_derive<NSOL>(P, ph, so_cur, dcur);
     }
     for (int z = z0; z < z1; z++) {
-        // Issue this plane's halo loads and the next plane's own loads first.
-        float hph[3] = {0.f, 0.f, 0.f};
-        float2 hso[NSOL];
-        if (has_halo) pf_load_raw<NSOL>(phase, sol_in, N, hcol + plane * z, hph, hso);
-        const bool need_next = use_z || (z + 1 < z1);
-        float nph[3] = {0.f, 0.f, 0.f};
-        if (need_next) pf_load_raw<NSOL>(phase, sol_in, N, col + plane * pf_mod(z + 1, iz), nph, so_nxt);
+        // Raw data of plane z (halo) and z+1 (own) must have landed; plane z+2
+        // goes in flight into the stage plane z-1 used.
+        issue(z + 2);
+        pf_cp_wait1();
 #pragma unroll
         for (int p = 0; p < 3; p++) {
-            sm_s[p][ly + 1][lx + 1] = dcur.s[p];
+            sm.ds[p][ly + 1][lx + 1] = dcur.s[p];
 #pragma unroll
-            for (int q = 0; q < NSOL; q++) sm_c[q][p][ly + 1][lx + 1] = dcur.c[q][p];
+            for (int q = 0; q < NSOL; q++) sm.dc[q][p][ly + 1][lx + 1] = dcur.c[q][p];
         }
         if (has_halo) {
+            const int st = (z - zlo) % NST;
+            const float hph[3] = {sm.hph[st][0][tid], sm.hph[st][1][tid], sm.hph[st][2][tid]};
+            float2 hso[NSOL];
+            pf_unpack_sol<NSOL>(sm.hso[st][tid], hso);
             pf_der<NSOL> dh;
             pf_derive<NSOL>(P, hph, hso, dh);
 #pragma unroll
             for (int p = 0; p < 3; p++) {
-                sm_s[p][hy + 1][hx + 1] = dh.s[p];
+                sm.ds[p][hy + 1][hx + 1] = dh.s[p];
 #pragma unroll
-                for (int q = 0; q < NSOL; q++) sm_c[q][p][hy + 1][hx + 1] = dh.c[q][p];
+                for (int q = 0; q < NSOL; q++) sm.dc[q][p][hy + 1][hx + 1] = dh.c[q][p];
             }
         }
         __syncthreads();
-        if (need_next) pf_derive<NSOL>(P, nph, so_nxt, dnext);
+        float2 so_nxt[NSOL];
+        const bool have_next = z + 1 <= zhi;
+        if (have_next) {
+            float nph[3];
+            own_raw(z + 1, nph, so_nxt);
+            pf_derive<NSOL>(P, nph, so_nxt, dnext);
+        }
         float acc[NSOL][3];
 #pragma unroll
         for (int p = 0; p < 3; p++) {
 #pragma unroll
             for (int q = 0; q < NSOL; q++) {
                 const float c0 = dcur.c[q][p];
-                float a = sm_s[p][ly + 1][lx] * (sm_c[q][p][ly + 1][lx] - c0);
-                a += sm_s[p][ly + 1][lx + 2] * (sm_c[q][p][ly + 1][lx + 2] - c0);
+                float a = sm.ds[p][ly + 1][lx] * (sm.dc[q][p][ly + 1][lx] - c0);
+                a += sm.ds[p][ly + 1][lx + 2] * (sm.dc[q][p][ly + 1][lx + 2] - c0);
                 if (use_y) {
-                    a += sm_s[p][ly][lx + 1] * (sm_c[q][p][ly][lx + 1] - c0);
-                    a += sm_s[p][ly + 2][lx + 1] * (sm_c[q][p][ly + 2][lx + 1] - c0);
+                    a += sm.ds[p][ly][lx + 1] * (sm.dc[q][p][ly][lx + 1] - c0);
+                    a += sm.ds[p][ly + 2][lx + 1] * (sm.dc[q][p][ly + 2][lx + 1] - c0);
                 }
                 if (use_z) {
                     a += dprev.s[p] * (dprev.c[q][p] - c0);
@@ -559,18 +649,27 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
     return cudaGetLastError();
 }
 
-cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *phase, const float2 *sol_in,
-                                  float2 *sol_out, cudaStream_t s) {
-    constexpr int TX = 32, TY = 8;
+template <int NSOL, int TX, int TY>
+static cudaError_t pf_launch_diffuse_tiled(const pf_f32_params &P, const float *phase, const float2 *sol_in,
+                                           float2 *sol_out, cudaStream_t s) {
     const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
     // z chunk: enough blocks for several waves on 152 SMs, at least 8 planes
-    // per block to amortise the two extra planes of the prologue.
+    // per block to amortise the extra planes of the prologue.
     int zchunk = P.iz;
     while (zchunk > 8 && (long long)tiles * ((P.iz + zchunk - 1) / zchunk) < 152 * 16) zchunk = (zchunk + 1) / 2;
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
-    if (P.nsol == 2)
-        k_diffuse_f32<2, TX, TY><<<grid, TX * TY, 0, s>>>(P, phase, sol_in, sol_out, zchunk);
-    else
-        k_diffuse_f32<1, TX, TY><<<grid, TX * TY, 0, s>>>(P, phase, sol_in, sol_out, zchunk);
+    const size_t smem = sizeof(pf_diff_smem<NSOL, TX, TY, 3>);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_diffuse_f32<NSOL, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    k_diffuse_f32<NSOL, TX, TY><<<grid, TX * TY, smem, s>>>(P, phase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
+}
+
+cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *phase, const float2 *sol_in,
+                                  float2 *sol_out, cudaStream_t s) {
+    if (P.nsol == 2) return pf_launch_diffuse_tiled<2, 32, 8>(P, phase, sol_in, sol_out, s);
+    return pf_launch_diffuse_tiled<1, 32, 8>(P, phase, sol_in, sol_out, s);
 }
