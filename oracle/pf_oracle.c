@@ -111,11 +111,13 @@ void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
             M3(p->k[0], i, j) = M3(p->dcdT, j, i) / M3(p->dcdT, i, j);
             M3(p->c[0], i, j) = M3(p->eq, j, i) - M3(p->k[0], i, j) * M3(p->eq, i, j);
         }
-    /* Mn (no reference counterpart): linear partition c_i = (r_i/r_j) c_j. */
+    /* Mn (no reference counterpart): c_p proportional to r_p.  In the sense of
+     * solver.cpp:389-405, k_ij is defined by c_j = k_ij*c_i + c_ij, so
+     * k_ij = r_j/r_i and c_ij = 0. */
     if (m->nsol > 1)
         for (int i = 1; i <= 3; i++)
             for (int j = 1; j <= 3; j++) {
-                M3(p->k[1], i, j) = m->mn_ratio[i - 1] / m->mn_ratio[j - 1];
+                M3(p->k[1], i, j) = m->mn_ratio[j - 1] / m->mn_ratio[i - 1];
                 M3(p->c[1], i, j) = 0.;
             }
     /* phase_field.cpp:247-248 */

@@ -294,10 +294,12 @@ void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
             p.k[0][e3(i, j)] = p.dcdT[e3(j, i)] / p.dcdT[e3(i, j)];
             p.c[0][e3(i, j)] = p.eq[e3(j, i)] - p.k[0][e3(i, j)] * p.eq[e3(i, j)];
         }
+    // Mn: c_p proportional to mn_ratio[p].  Partitioning (solver.cpp:389-405)
+    // reads k_ij as c_j = k_ij*c_i + c_ij, hence k_ij = r_j/r_i, c_ij = 0.
     if (m.nsol > 1)
         for (int i = 1; i <= 3; i++)
             for (int j = 1; j <= 3; j++) {
-                p.k[1][e3(i, j)] = m.mn_ratio[i - 1] / m.mn_ratio[j - 1];
+                p.k[1][e3(i, j)] = m.mn_ratio[j - 1] / m.mn_ratio[i - 1];
                 p.c[1][e3(i, j)] = 0.;
             }
     // phase_field.cpp:247-248

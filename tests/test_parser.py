@@ -96,7 +96,7 @@ def test_parameters_known_answer():
     assert np.isclose(p.k[0][3], dcdT21 / dcdT12)            # k(1,2)
     eq12, eq21 = -1e-4 * T + 0.11, -5e-3 * T + 5.395
     assert np.isclose(p.c[0][3], eq21 - (dcdT21 / dcdT12) * eq12)
-    assert p.k[1][1] == 2.0 and p.k[1][3] == 0.5             # Mn: k(2,1) = r2/r1
+    assert p.k[1][1] == 0.5 and p.k[1][3] == 2.0             # Mn: k(2,1) = r1/r2, k(1,2) = r2/r1
     assert p.nnb == 4
 
 
