@@ -221,6 +221,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     F = pf.PhaseField(m, pf.PF_PREC_FP32C)
     F.set_stream(stream.cuda_stream)
     F.upload(st0, 0.0)
+    tuned = F.autotune() if not args.no_tune else None
     F.update(args.warmup)
     F.enable_kernel_timing(True)
     barrier()
@@ -263,7 +264,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                 "phase_ms": kt64["phase"][0] / max(1, kt64["phase"][1]),
                 "diffusion_ms": kt64["diffusion"][0] / max(1, kt64["diffusion"][1])}
     if args.no_e2e:
-        return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk)
+        return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk, tuned)
 
     # ---- e2e: through the C ABI with pinned host buffers -----------------
     keep_alive = []
@@ -280,7 +281,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     back = {k: pinned(np.zeros_like(v)) for k, v in st0.items()}
     H = pf.PhaseField(m, pf.PF_PREC_FP32C)
     H.set_stream(stream.cuda_stream)
-    H.upload(host, 0.0)   # warm the path (allocations, module load)
+    H.upload(host, 0.0)   # warm the path (allocations, module load) and tune once
+    if not args.no_tune:
+        H.autotune()
     H.update(1)
     torch.cuda.synchronize()
     barrier()
@@ -299,10 +302,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     e2e = {"value": world * N * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(state_bytes / args.steps),
            "d2h_bytes_per_step": int(64 + down_bytes / args.steps)}
-    return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk)
+    return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned)
 
 
-def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk):
+def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned=None):
     if rank != 0:
         return None
     pk = _peaks()
@@ -350,6 +353,7 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
             "diffusion_f32": {"launches": kt["diffusion"][1], "mean_ms": t_diff * 1e3, "gbs": ach,
                               "bytes_per_launch": diff_bytes},
             "step_gbs_effective": step_bytes * args.steps / (ms / 1e3) / 1e9,
+            "diffusion_tile": tuned,
         },
         "fp64": fp64,
         "fp32_over_fp64": (value / fp64["value"]) if fp64 else None,
@@ -371,6 +375,7 @@ def main() -> None:
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the diffusion tile autotuner")
     ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -45,13 +45,14 @@ NVCC_FLAGS = ARCH + [
 PER_FILE = {
     "pf_f64.cu": ["-fmad=false"],
     "pf_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "pf_f32_diffuse.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
              "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_reduce.cu", "pf_api.cu", "pf_reduce_noalloc.cu"]
+CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_reduce.cu", "pf_api.cu", "pf_reduce_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
-HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_kernels.h", "pf_host.h"]
+HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

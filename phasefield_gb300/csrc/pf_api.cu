@@ -161,6 +161,10 @@ struct pf_ctx {
     cudaGraphExec_t gexec = nullptr;
     pf_step_params gparams{};
     int gphase = -1;
+    // diffusion tile shape chosen by pf_autotune (FP32C)
+    pf_diff_cfg diff_cfg{8, 16};
+    bool diff_cfg_valid = false;
+    float diff_cfg_ms = 0.f;
 };
 
 namespace {
@@ -252,7 +256,7 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         for (int it = 0; it < P.n_sub; it++) {
             const int b = c->curs;
             e = timed(c, 1, [&] {
-                return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream);
+                return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream, c->diff_cfg_valid ? &c->diff_cfg : nullptr);
             });
             if (e != cudaSuccess) return e;
             c->curs = 1 - b;
@@ -542,11 +546,64 @@ extern "C" int pf_diffuse(pf_ctx *c, int nsub) {
         pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
         for (int it = 0; it < nsub && e == cudaSuccess; it++) {
             const int b = c->curs;
-            e = timed(c, 1, [&] { return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream); });
+            e = timed(c, 1, [&] { return pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream, c->diff_cfg_valid ? &c->diff_cfg : nullptr); });
             c->curs = 1 - b;
         }
     }
     return e == cudaSuccess ? PF_OK : pf_cuda_fail(e);
+}
+
+// Autotuner of the FP32 diffusion tile shape: every candidate (tile height x
+// z chunk) runs on the context's own state, reading the current solute buffer
+// and writing the spare one (which the next sub-step overwrites anyway), and
+// the fastest mean of three timed launches is kept for this context.
+extern "C" int pf_autotune(pf_ctx *c, int *ty, int *zchunk, float *ms) {
+    if (!c || !c->have_state) return pf_fail(PF_ERR_ARG, "pf_autotune: no state uploaded");
+    if (c->prec != PF_PREC_FP32C) {
+        if (ty) *ty = 0;
+        if (zchunk) *zchunk = 0;
+        if (ms) *ms = 0.f;
+        return PF_OK;
+    }
+    pf_step_params P;
+    pf_compute_params(c->model, c->time, P);
+    pf_f32_params F;
+    pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
+    pf_diff_cfg cand[32];
+    const int nc = pf_diffuse_candidates(F, cand, 32);
+    cudaEvent_t e0, e1;
+    PF_CUDA_OK(cudaEventCreate(&e0));
+    PF_CUDA_OK(cudaEventCreate(&e1));
+    const int b = c->curs;
+    float best = 1e30f;
+    pf_diff_cfg best_cfg = pf_diffuse_default_cfg(F);
+    int st = PF_OK;
+    for (int i = 0; i < nc && st == PF_OK; i++) {
+        cudaError_t e = pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream, &cand[i]);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 3 && e == cudaSuccess; r++)
+            e = pf_launch_diffuse_f32(F, c->phase32, c->sol[b], c->sol[1 - b], c->stream, &cand[i]);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (e != cudaSuccess) st = pf_cuda_fail(e);
+        else if (t / 3 < best) {
+            best = t / 3;
+            best_cfg = cand[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != PF_OK) return st;
+    c->diff_cfg = best_cfg;
+    c->diff_cfg_valid = true;
+    c->diff_cfg_ms = best;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    if (ty) *ty = best_cfg.ty;
+    if (zchunk) *zchunk = best_cfg.zchunk;
+    if (ms) *ms = best;
+    return PF_OK;
 }
 
 extern "C" int pf_reduce(pf_ctx *c, double out[8]) {

@@ -342,6 +342,19 @@ void pf_fold_f32(const pf_step_params &p, int b1, int b2, pf_f32_params &f) {
             f.k[q][e] = (float)p.k[q][e];
             f.c[q][e] = (float)p.c[q][e];
         }
+        // Separable partition?  a_j = k_1j (a_1 = 1); require c_ij = 0 and
+        // k_ij = a_j/a_i to 1e-12 relative.
+        bool sep = true;
+        double a[3];
+        for (int j = 1; j <= 3; j++) a[j - 1] = p.k[q][e3(1, j)];
+        for (int i = 1; i <= 3 && sep; i++)
+            for (int j = 1; j <= 3 && sep; j++) {
+                const double kij = p.k[q][e3(i, j)], want = a[j - 1] / a[i - 1];
+                if (p.c[q][e3(i, j)] != 0.0 || !(std::abs(kij - want) <= 1e-12 * std::abs(want)) || a[i - 1] <= 0.0)
+                    sep = false;
+            }
+        f.sep[q] = sep ? 1 : 0;
+        for (int j = 0; j < 3; j++) f.a[q][j] = sep ? (float)a[j] : 0.f;
     }
 }
 

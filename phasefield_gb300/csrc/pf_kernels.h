@@ -32,8 +32,17 @@ cudaError_t pf_launch_unpack_f32(const pf_step_params &P, const pf_f32_map &map,
 cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, const float4 *phi1,
                                 ushort4 *gid2, float4 *phi2, float *phase, const float2 *sol,
                                 cudaStream_t s);
-cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *phase, const float2 *sol_in,
-                                  float2 *sol_out, cudaStream_t s);
+// Tile shape of the diffusion kernel: TX = 32 cells in x, ty in y, zchunk z
+// planes per block (chosen by the autotuner or the default rule).
+struct pf_diff_cfg {
+    int ty;
+    int zchunk;
+};
+pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P);
+int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max);
+// 'sphase' holds the square roots of the phase fractions (pf_f32.cuh).
+cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, const float2 *sol_in,
+                                  float2 *sol_out, cudaStream_t s, const pf_diff_cfg *cfg);
 
 // ---- FP64 reductions (pf_reduce.cu) ----
 // out[0..2]  sum of phase fractions, out[3] sum of phi over slots whose grain

@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_f32(long long N, int nso
          n += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int p = 0; p < 3; p++) {
-            const double v = (double)phase[p * N + n];
+            const double sq = (double)phase[p * N + n];  // planes hold sqrt(phase fraction)
+            const double v = sq * sq;
             acc[p] += v;
             acc[7] += nf(v);
         }

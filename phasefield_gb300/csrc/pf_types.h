@@ -38,4 +38,7 @@ typedef struct {
     // solver.cpp:246) and G is zero on the diagonal (solver.cpp:381).
     float D[PF_MAXSOL][3];      // D * dt_sub/dx^2
     float k[PF_MAXSOL][9], c[PF_MAXSOL][9];
+    // Separable partition of solute q (c_ij = 0, k_ij = a_j/a_i): c_i = a_i C / sum_j phi_j a_j.
+    int sep[PF_MAXSOL];
+    float a[PF_MAXSOL][3];
 } pf_f32_params;
