@@ -135,7 +135,8 @@ SYMBOLS = {
     "pf_enable_kernel_timing": (_I, [_P, _I]),
     "pf_kernel_times": (_I, [_P, _DP, ctypes.POINTER(ctypes.c_longlong)]),
     "pf_use_graph": (_I, [_P, _I]),
-    "pf_autotune": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float)]),
+    "pf_autotune": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                         ctypes.POINTER(ctypes.c_float)]),
     "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
     "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
     "pf_reduce_noalloc": (_I, [ctypes.c_longlong, _I, _P, _P, _P, _P, _P, _P]),
@@ -308,9 +309,10 @@ class PhaseField:
 
     def autotune(self) -> dict:
         """Pick the FP32C diffusion tile shape by timing the candidates on this state."""
-        ty, zc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
-        check(lib().pf_autotune(self._ctx, ctypes.byref(ty), ctypes.byref(zc), ctypes.byref(ms)), "pf_autotune")
-        return {"tile_y": ty.value, "zchunk": zc.value, "ms": ms.value}
+        ty, zc, d, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        check(lib().pf_autotune(self._ctx, ctypes.byref(ty), ctypes.byref(zc), ctypes.byref(d), ctypes.byref(ms)),
+              "pf_autotune")
+        return {"tile_y": ty.value, "zchunk": zc.value, "depth": d.value, "ms": ms.value}
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(lib().pf_set_stream(self._ctx, ctypes.c_void_p(stream_handle) if stream_handle else None),

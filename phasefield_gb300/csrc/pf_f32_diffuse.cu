@@ -37,7 +37,8 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+template <int PENDING>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING)); }
 
 template <int NSOL> struct Vec;
 template <> struct Vec<1> { using T = float2; };
@@ -78,9 +79,10 @@ __device__ __forceinline__ void derive(const pf_f32_params &P, const float s[3],
     for (int q = 0; q < NSOL; q++) pf_partition_q(P, q, C[q], ph, d.c[q]);
 }
 
-template <int NSOL, int TX, int TY>
+// D = prefetch depth in planes; D + 1 raw stages.
+template <int NSOL, int TX, int TY, int D>
 struct Smem {
-    static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2, NST = 3;
+    static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2, NST = D + 1;
     using SV = typename Vec<NSOL>::T;
     SV so[NST][NT];       // raw solute totals (+ compensation), own cells
     SV hso[NST][NH];      // raw solute totals, halo cells
@@ -89,14 +91,15 @@ struct Smem {
     SV rec[3][H][W];      // derived records of the current plane, with halo
 };
 
-template <int NSOL, int NNB, int TX, int TY>
+template <int NSOL, int NNB, int TX, int TY, int D>
 __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __grid_constant__ pf_f32_params P,
                                                                      const float *__restrict__ sphase,
                                                                      const float2 *__restrict__ sol_in,
                                                                      float2 *__restrict__ sol_out, int zchunk) {
-    using S = Smem<NSOL, TX, TY>;
+    using S = Smem<NSOL, TX, TY, D>;
     using SV = typename Vec<NSOL>::T;
-    static_assert(S::NH <= S::NT, "halo needs one thread per halo cell");
+    constexpr int NW = S::NT / 32;  // warps per block
+    static_assert((S::NH + NW - 1) / NW <= 32, "halo needs one thread per halo cell");
     constexpr bool use_y = NNB >= 4, use_z = NNB >= 6;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S &sm = *reinterpret_cast<S *>(smem_raw);
@@ -113,12 +116,15 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     // Every shared slot holds the cell at the wrapped coordinates, so partial
     // tiles and periodic neighbours need no special case.
     const long long col = pf_mod(tx0 + lx, ix) + (long long)ix * pf_mod(ty0 + ly, iy);
-    const bool has_halo = tid < S::NH;
+    // Halo cells are dealt round-robin to the warps (lanes 0..NH/NW of every
+    // warp), so each warp does the same extra work before the barrier.
+    const int hid = (tid % 32) * NW + tid / 32;
+    const bool has_halo = hid < S::NH;
     int hx, hy;
-    if (tid < TX) { hx = tid; hy = -1; }
-    else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
-    else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
-    else { hx = TX; hy = tid - 2 * TX - TY; }
+    if (hid < TX) { hx = hid; hy = -1; }
+    else if (hid < 2 * TX) { hx = hid - TX; hy = TY; }
+    else if (hid < 2 * TX + TY) { hx = -1; hy = hid - 2 * TX; }
+    else { hx = TX; hy = hid - 2 * TX - TY; }
     const long long hcol = pf_mod(tx0 + hx, ix) + (long long)ix * pf_mod(ty0 + hy, iy);
     const int z0 = blockIdx.y * zchunk;
     const int z1 = min(z0 + zchunk, iz);
@@ -140,11 +146,11 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
             if (NSOL == 2) cp_async16(&sm.so[st][tid], own_v + off);
             else cp_async8(&sm.so[st][tid], own_v + off);
             if (has_halo && zz >= z0 && zz < z1) {
-                cp_async4(&sm.hsp[st][0][tid], halo_s + off);
-                cp_async4(&sm.hsp[st][1][tid], halo_s + N + off);
-                cp_async4(&sm.hsp[st][2][tid], halo_s + 2 * N + off);
-                if (NSOL == 2) cp_async16(&sm.hso[st][tid], halo_v + off);
-                else cp_async8(&sm.hso[st][tid], halo_v + off);
+                cp_async4(&sm.hsp[st][0][hid], halo_s + off);
+                cp_async4(&sm.hsp[st][1][hid], halo_s + N + off);
+                cp_async4(&sm.hsp[st][2][hid], halo_s + 2 * N + off);
+                if (NSOL == 2) cp_async16(&sm.hso[st][hid], halo_v + off);
+                else cp_async8(&sm.hso[st][hid], halo_v + off);
             }
         }
         cp_commit();
@@ -159,8 +165,8 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
 
     // One plane.  prev/cur/next rotate through the unrolled loop below.
     auto body = [&](int z, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
-        issue(z + 2);
-        cp_wait1();  // planes z (halo) and z+1 (own) have landed
+        issue(z + D);
+        cp_wait<D - 1>();  // planes z (halo) and z+1 (own) have landed
 #pragma unroll
         for (int p = 0; p < 3; p++) {
             float cp[NSOL];
@@ -170,9 +176,9 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
         }
         if (has_halo) {
             const int st = stage(z);
-            const float s3[3] = {sm.hsp[st][0][tid], sm.hsp[st][1][tid], sm.hsp[st][2][tid]};
+            const float s3[3] = {sm.hsp[st][0][hid], sm.hsp[st][1][hid], sm.hsp[st][2][hid]};
             float C[NSOL], comp[NSOL];
-            unpack_sol<NSOL>(sm.hso[st][tid], C, comp);
+            unpack_sol<NSOL>(sm.hso[st][hid], C, comp);
             Der<NSOL> dh;
             derive<NSOL>(P, s3, C, dh);
 #pragma unroll
@@ -228,10 +234,9 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     };
 
     Der<NSOL> A, B, Cd;
-    issue(zlo);
-    issue(zlo + 1);
-    if (use_z) issue(zlo + 2);
-    cp_wait1();
+    // Planes zlo .. z0+D-1 in flight; zlo and z0 must have landed.
+    for (int zz = zlo; zz <= z0 + D - 1; zz++) issue(zz);
+    cp_wait<D - 1>();
     if (use_z) derive_own(z0 - 1, A);
     derive_own(z0, B);
     for (int z = z0; z < z1; z += 3) {
@@ -241,40 +246,47 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     }
 }
 
-template <int NSOL, int NNB, int TY>
+template <int NSOL, int NNB, int TY, int D>
 cudaError_t launch_one(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
                        cudaStream_t s, int zchunk) {
     constexpr int TX = 32;
-    using S = Smem<NSOL, TX, TY>;
+    using S = Smem<NSOL, TX, TY, D>;
     const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY>,
+        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY, D>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    k_diffuse<NSOL, NNB, TX, TY><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
+    k_diffuse<NSOL, NNB, TX, TY, D><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
 }
 
 template <int NSOL, int NNB>
 cudaError_t launch_ty(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
-                      cudaStream_t s, int ty, int zchunk) {
+                      cudaStream_t s, int ty, int zchunk, int depth) {
+    if (depth >= 3) {
+        switch (ty) {
+            case 4: return launch_one<NSOL, NNB, 4, 3>(P, sphase, sol_in, sol_out, s, zchunk);
+            case 16: return launch_one<NSOL, NNB, 16, 3>(P, sphase, sol_in, sol_out, s, zchunk);
+            default: return launch_one<NSOL, NNB, 8, 3>(P, sphase, sol_in, sol_out, s, zchunk);
+        }
+    }
     switch (ty) {
-        case 4: return launch_one<NSOL, NNB, 4>(P, sphase, sol_in, sol_out, s, zchunk);
-        case 16: return launch_one<NSOL, NNB, 16>(P, sphase, sol_in, sol_out, s, zchunk);
-        default: return launch_one<NSOL, NNB, 8>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 4: return launch_one<NSOL, NNB, 4, 2>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 16: return launch_one<NSOL, NNB, 16, 2>(P, sphase, sol_in, sol_out, s, zchunk);
+        default: return launch_one<NSOL, NNB, 8, 2>(P, sphase, sol_in, sol_out, s, zchunk);
     }
 }
 
 template <int NSOL>
 cudaError_t launch_nnb(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
-                       cudaStream_t s, int ty, int zchunk) {
-    if (P.nnb >= 6) return launch_ty<NSOL, 6>(P, sphase, sol_in, sol_out, s, ty, zchunk);
-    if (P.nnb >= 4) return launch_ty<NSOL, 4>(P, sphase, sol_in, sol_out, s, ty, zchunk);
-    return launch_ty<NSOL, 2>(P, sphase, sol_in, sol_out, s, ty, zchunk);
+                       cudaStream_t s, int ty, int zchunk, int depth) {
+    if (P.nnb >= 6) return launch_ty<NSOL, 6>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
+    if (P.nnb >= 4) return launch_ty<NSOL, 4>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
+    return launch_ty<NSOL, 2>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
 }
 
 }  // namespace
@@ -282,6 +294,7 @@ cudaError_t launch_nnb(const pf_f32_params &P, const float *sphase, const float2
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P) {
     pf_diff_cfg c;
     c.ty = 8;
+    c.depth = 2;
     const int tiles = ((P.ix + 31) / 32) * ((P.iy + 7) / 8);
     // About two waves of 4 resident blocks on 152 SMs, at least 8 planes per block.
     int z = P.iz;
@@ -294,22 +307,23 @@ int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max) {
     const int tys[3] = {4, 8, 16};
     const int zcs[5] = {8, 16, 32, 64, 128};
     int n = 0;
-    for (int a = 0; a < 3; a++) {
-        if (P.iz == 1) {
-            if (n < max) out[n++] = {tys[a], 1};
-            continue;
+    for (int d = 2; d <= 3; d++)
+        for (int a = 0; a < 3; a++) {
+            if (P.iz == 1) {
+                if (n < max) out[n++] = {tys[a], 1, d};
+                continue;
+            }
+            for (int b = 0; b < 5; b++) {
+                if (zcs[b] > P.iz && b > 0) break;
+                if (n < max) out[n++] = {tys[a], zcs[b] < P.iz ? zcs[b] : P.iz, d};
+            }
         }
-        for (int b = 0; b < 5; b++) {
-            if (zcs[b] > P.iz && b > 0) break;
-            if (n < max) out[n++] = {tys[a], zcs[b] < P.iz ? zcs[b] : P.iz};
-        }
-    }
     return n;
 }
 
 cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, const float2 *sol_in,
                                   float2 *sol_out, cudaStream_t s, const pf_diff_cfg *cfg) {
     const pf_diff_cfg c = cfg ? *cfg : pf_diffuse_default_cfg(P);
-    if (P.nsol == 2) return launch_nnb<2>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk);
-    return launch_nnb<1>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk);
+    if (P.nsol == 2) return launch_nnb<2>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.depth);
+    return launch_nnb<1>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.depth);
 }
