@@ -198,8 +198,9 @@ int pf_kernel_times(pf_ctx *ctx, double times_ms[2], long long counts[2]);
 int pf_use_graph(pf_ctx *ctx, int on);
 /* Time every candidate tile shape of the FP32C diffusion kernel on the
  * context's own state and keep the fastest (state unchanged); reports the
- * chosen tile height, z chunk, prefetch depth and mean launch time.  No-op for FP64. */
-int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *depth, float *ms);
+ * chosen tile height, z chunk, kernel variant (0: two barriers per plane, 1:
+ * double-buffered records) and mean launch time.  No-op for FP64. */
+int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *variant, float *ms);
 /* Reference output writers (write_data.cpp:3-82).  pf_write_data appends a
  * fraction_time.txt row under 'directory' when the reference would (or when
  * forced) and, if the model's micro_out flag is set, writes a VTI file. */

@@ -312,7 +312,7 @@ class PhaseField:
         ty, zc, d, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
         check(lib().pf_autotune(self._ctx, ctypes.byref(ty), ctypes.byref(zc), ctypes.byref(d), ctypes.byref(ms)),
               "pf_autotune")
-        return {"tile_y": ty.value, "zchunk": zc.value, "depth": d.value, "ms": ms.value}
+        return {"tile_y": ty.value, "zchunk": zc.value, "variant": d.value, "ms": ms.value}
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(lib().pf_set_stream(self._ctx, ctypes.c_void_p(stream_handle) if stream_handle else None),

@@ -162,7 +162,7 @@ struct pf_ctx {
     pf_step_params gparams{};
     int gphase = -1;
     // diffusion tile shape chosen by pf_autotune (FP32C)
-    pf_diff_cfg diff_cfg{8, 16, 2};
+    pf_diff_cfg diff_cfg{8, 16, 0};
     bool diff_cfg_valid = false;
     float diff_cfg_ms = 0.f;
 };
@@ -557,12 +557,12 @@ extern "C" int pf_diffuse(pf_ctx *c, int nsub) {
 // z chunk) runs on the context's own state, reading the current solute buffer
 // and writing the spare one (which the next sub-step overwrites anyway), and
 // the fastest mean of three timed launches is kept for this context.
-extern "C" int pf_autotune(pf_ctx *c, int *ty, int *zchunk, int *depth, float *ms) {
+extern "C" int pf_autotune(pf_ctx *c, int *ty, int *zchunk, int *variant, float *ms) {
     if (!c || !c->have_state) return pf_fail(PF_ERR_ARG, "pf_autotune: no state uploaded");
     if (c->prec != PF_PREC_FP32C) {
         if (ty) *ty = 0;
         if (zchunk) *zchunk = 0;
-        if (depth) *depth = 0;
+        if (variant) *variant = 0;
         if (ms) *ms = 0.f;
         return PF_OK;
     }
@@ -603,7 +603,7 @@ extern "C" int pf_autotune(pf_ctx *c, int *ty, int *zchunk, int *depth, float *m
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
     if (ty) *ty = best_cfg.ty;
     if (zchunk) *zchunk = best_cfg.zchunk;
-    if (depth) *depth = best_cfg.depth;
+    if (variant) *variant = best_cfg.variant;
     if (ms) *ms = best;
     return PF_OK;
 }

@@ -79,27 +79,28 @@ __device__ __forceinline__ void derive(const pf_f32_params &P, const float s[3],
     for (int q = 0; q < NSOL; q++) pf_partition_q(P, q, C[q], ph, d.c[q]);
 }
 
-// D = prefetch depth in planes; D + 1 raw stages.
-template <int NSOL, int TX, int TY, int D>
+// Raw data is prefetched two planes ahead (three stages).  DB: the derived
+// records are double-buffered by plane parity, which saves the second barrier
+// of every plane at the cost of shared memory (3 instead of 4 resident blocks).
+template <int NSOL, int TX, int TY, bool DB>
 struct Smem {
-    static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2, NST = D + 1;
+    static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2, NST = 3;
     using SV = typename Vec<NSOL>::T;
     SV so[NST][NT];       // raw solute totals (+ compensation), own cells
     SV hso[NST][NH];      // raw solute totals, halo cells
     float sp[NST][3][NT];  // raw s_p, own cells
     float hsp[NST][3][NH]; // raw s_p, halo cells
-    SV rec[3][H][W];      // derived records of the current plane, with halo
+    SV rec[DB ? 2 : 1][3][H][W];  // derived records of the current plane, with halo
 };
 
-template <int NSOL, int NNB, int TX, int TY, int D>
-__global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __grid_constant__ pf_f32_params P,
+template <int NSOL, int NNB, int TX, int TY, bool DB>
+__global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffuse(const __grid_constant__ pf_f32_params P,
                                                                      const float *__restrict__ sphase,
                                                                      const float2 *__restrict__ sol_in,
                                                                      float2 *__restrict__ sol_out, int zchunk) {
-    using S = Smem<NSOL, TX, TY, D>;
+    using S = Smem<NSOL, TX, TY, DB>;
     using SV = typename Vec<NSOL>::T;
-    constexpr int NW = S::NT / 32;  // warps per block
-    static_assert((S::NH + NW - 1) / NW <= 32, "halo needs one thread per halo cell");
+    static_assert(S::NH <= S::NT, "halo needs one thread per halo cell");
     constexpr bool use_y = NNB >= 4, use_z = NNB >= 6;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S &sm = *reinterpret_cast<S *>(smem_raw);
@@ -116,9 +117,9 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     // Every shared slot holds the cell at the wrapped coordinates, so partial
     // tiles and periodic neighbours need no special case.
     const long long col = pf_mod(tx0 + lx, ix) + (long long)ix * pf_mod(ty0 + ly, iy);
-    // Halo cells are dealt round-robin to the warps (lanes 0..NH/NW of every
-    // warp), so each warp does the same extra work before the barrier.
-    const int hid = (tid % 32) * NW + tid / 32;
+    // Halo cells go to the first NH threads: whole rows to whole warps, so the
+    // halo copies stay coalesced.
+    const int hid = tid;
     const bool has_halo = hid < S::NH;
     int hx, hy;
     if (hid < TX) { hx = hid; hy = -1; }
@@ -165,14 +166,15 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
 
     // One plane.  prev/cur/next rotate through the unrolled loop below.
     auto body = [&](int z, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
-        issue(z + D);
-        cp_wait<D - 1>();  // planes z (halo) and z+1 (own) have landed
+        issue(z + 2);
+        cp_wait<1>();  // planes z (halo) and z+1 (own) have landed
+        const int rb = DB ? (z & 1) : 0;
 #pragma unroll
         for (int p = 0; p < 3; p++) {
             float cp[NSOL];
 #pragma unroll
             for (int q = 0; q < NSOL; q++) cp[q] = cur.c[q][p];
-            sm.rec[p][ly + 1][lx + 1] = pack_rec<NSOL>(cur.s[p], cp);
+            sm.rec[rb][p][ly + 1][lx + 1] = pack_rec<NSOL>(cur.s[p], cp);
         }
         if (has_halo) {
             const int st = stage(z);
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
                 float cp[NSOL];
 #pragma unroll
                 for (int q = 0; q < NSOL; q++) cp[q] = dh.c[q][p];
-                sm.rec[p][hy + 1][hx + 1] = pack_rec<NSOL>(dh.s[p], cp);
+                sm.rec[rb][p][hy + 1][hx + 1] = pack_rec<NSOL>(dh.s[p], cp);
             }
         }
         __syncthreads();
@@ -194,9 +196,9 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
         float acc[NSOL][3];
 #pragma unroll
         for (int p = 0; p < 3; p++) {
-            const SV l = sm.rec[p][ly + 1][lx], r = sm.rec[p][ly + 1][lx + 2];
+            const SV l = sm.rec[rb][p][ly + 1][lx], r = sm.rec[rb][p][ly + 1][lx + 2];
             SV d, u;
-            if (use_y) { d = sm.rec[p][ly][lx + 1]; u = sm.rec[p][ly + 2][lx + 1]; }
+            if (use_y) { d = sm.rec[rb][p][ly][lx + 1]; u = sm.rec[rb][p][ly + 2][lx + 1]; }
 #pragma unroll
             for (int q = 0; q < NSOL; q++) {
                 const float c0 = cur.c[q][p];
@@ -230,13 +232,13 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
             if (NSOL == 2) reinterpret_cast<float4 *>(sol_out)[n] = make_float4(o[0], o[1], o[2], o[2 * NSOL - 1]);
             else sol_out[n] = make_float2(o[0], o[1]);
         }
-        __syncthreads();
+        if (!DB) __syncthreads();
     };
 
     Der<NSOL> A, B, Cd;
-    // Planes zlo .. z0+D-1 in flight; zlo and z0 must have landed.
-    for (int zz = zlo; zz <= z0 + D - 1; zz++) issue(zz);
-    cp_wait<D - 1>();
+    // Planes zlo .. z0+1 in flight; zlo and z0 must have landed.
+    for (int zz = zlo; zz <= z0 + 1; zz++) issue(zz);
+    cp_wait<1>();
     if (use_z) derive_own(z0 - 1, A);
     derive_own(z0, B);
     for (int z = z0; z < z1; z += 3) {
@@ -246,47 +248,47 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     }
 }
 
-template <int NSOL, int NNB, int TY, int D>
+template <int NSOL, int NNB, int TY, bool DB>
 cudaError_t launch_one(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
                        cudaStream_t s, int zchunk) {
     constexpr int TX = 32;
-    using S = Smem<NSOL, TX, TY, D>;
+    using S = Smem<NSOL, TX, TY, DB>;
     const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY, D>,
+        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY, DB>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    k_diffuse<NSOL, NNB, TX, TY, D><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
+    k_diffuse<NSOL, NNB, TX, TY, DB><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
 }
 
 template <int NSOL, int NNB>
 cudaError_t launch_ty(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
-                      cudaStream_t s, int ty, int zchunk, int depth) {
-    if (depth >= 3) {
+                      cudaStream_t s, int ty, int zchunk, int variant) {
+    if (variant == 1) {
         switch (ty) {
-            case 4: return launch_one<NSOL, NNB, 4, 3>(P, sphase, sol_in, sol_out, s, zchunk);
-            case 16: return launch_one<NSOL, NNB, 16, 3>(P, sphase, sol_in, sol_out, s, zchunk);
-            default: return launch_one<NSOL, NNB, 8, 3>(P, sphase, sol_in, sol_out, s, zchunk);
+            case 4: return launch_one<NSOL, NNB, 4, true>(P, sphase, sol_in, sol_out, s, zchunk);
+            case 16: return launch_one<NSOL, NNB, 16, true>(P, sphase, sol_in, sol_out, s, zchunk);
+            default: return launch_one<NSOL, NNB, 8, true>(P, sphase, sol_in, sol_out, s, zchunk);
         }
     }
     switch (ty) {
-        case 4: return launch_one<NSOL, NNB, 4, 2>(P, sphase, sol_in, sol_out, s, zchunk);
-        case 16: return launch_one<NSOL, NNB, 16, 2>(P, sphase, sol_in, sol_out, s, zchunk);
-        default: return launch_one<NSOL, NNB, 8, 2>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 4: return launch_one<NSOL, NNB, 4, false>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 16: return launch_one<NSOL, NNB, 16, false>(P, sphase, sol_in, sol_out, s, zchunk);
+        default: return launch_one<NSOL, NNB, 8, false>(P, sphase, sol_in, sol_out, s, zchunk);
     }
 }
 
 template <int NSOL>
 cudaError_t launch_nnb(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
-                       cudaStream_t s, int ty, int zchunk, int depth) {
-    if (P.nnb >= 6) return launch_ty<NSOL, 6>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
-    if (P.nnb >= 4) return launch_ty<NSOL, 4>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
-    return launch_ty<NSOL, 2>(P, sphase, sol_in, sol_out, s, ty, zchunk, depth);
+                       cudaStream_t s, int ty, int zchunk, int variant) {
+    if (P.nnb >= 6) return launch_ty<NSOL, 6>(P, sphase, sol_in, sol_out, s, ty, zchunk, variant);
+    if (P.nnb >= 4) return launch_ty<NSOL, 4>(P, sphase, sol_in, sol_out, s, ty, zchunk, variant);
+    return launch_ty<NSOL, 2>(P, sphase, sol_in, sol_out, s, ty, zchunk, variant);
 }
 
 }  // namespace
@@ -294,7 +296,7 @@ cudaError_t launch_nnb(const pf_f32_params &P, const float *sphase, const float2
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P) {
     pf_diff_cfg c;
     c.ty = 8;
-    c.depth = 2;
+    c.variant = 0;
     const int tiles = ((P.ix + 31) / 32) * ((P.iy + 7) / 8);
     // About two waves of 4 resident blocks on 152 SMs, at least 8 planes per block.
     int z = P.iz;
@@ -307,7 +309,7 @@ int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max) {
     const int tys[3] = {4, 8, 16};
     const int zcs[5] = {8, 16, 32, 64, 128};
     int n = 0;
-    for (int d = 2; d <= 3; d++)
+    for (int d = 0; d <= 1; d++)
         for (int a = 0; a < 3; a++) {
             if (P.iz == 1) {
                 if (n < max) out[n++] = {tys[a], 1, d};
@@ -324,6 +326,6 @@ int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max) {
 cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, const float2 *sol_in,
                                   float2 *sol_out, cudaStream_t s, const pf_diff_cfg *cfg) {
     const pf_diff_cfg c = cfg ? *cfg : pf_diffuse_default_cfg(P);
-    if (P.nsol == 2) return launch_nnb<2>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.depth);
-    return launch_nnb<1>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.depth);
+    if (P.nsol == 2) return launch_nnb<2>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.variant);
+    return launch_nnb<1>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk, c.variant);
 }

@@ -33,11 +33,11 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
                                 ushort4 *gid2, float4 *phi2, float *phase, const float2 *sol,
                                 cudaStream_t s);
 // Tile shape of the diffusion kernel: TX = 32 cells in x, ty in y, zchunk z
-// planes per block, prefetch depth (chosen by the autotuner or the default rule).
+// planes per block, kernel variant (chosen by the autotuner or the default rule).
 struct pf_diff_cfg {
     int ty;
     int zchunk;
-    int depth;   // cp.async prefetch depth in planes (2 or 3)
+    int variant; // 0: two barriers per plane; 1: double-buffered records, one barrier
 };
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P);
 int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max);
