@@ -201,6 +201,28 @@ int pf_use_graph(pf_ctx *ctx, int on);
  * chosen tile height, z chunk, kernel variant (0: two barriers per plane, 1:
  * double-buffered records) and mean launch time.  No-op for FP64. */
 int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *variant, float *ms);
+/* Batched ensemble (no reference counterpart): many independent 2D domains
+ * (own size, constant temperature, time step, sub-step count), each stored
+ * like a PF_PREC_FP32C context, advanced together by one persistent
+ * cooperative kernel launch replayed from a CUDA graph.  Blocks are grouped per
+ * domain; a group's barrier waits are bounded (default 2 s), and a launch whose
+ * wait runs out is abandoned and reported as PF_ERR_TIMEOUT (the device stays
+ * usable; the domains' states must then be uploaded again). */
+typedef struct pf_batch pf_batch;
+int pf_batch_create(const pf_model *models, int ndomains, pf_batch **out);
+int pf_batch_upload(pf_batch *b, int domain, const int32_t *ids, const double *phi, const double *phase,
+                    const double *C, double time);
+int pf_batch_run(pf_batch *b, int nsteps);
+int pf_batch_download(pf_batch *b, int domain, int32_t *ids, double *phi, double *phase, double *conc,
+                      double *C, double *time);
+int pf_batch_reduce(pf_batch *b, int domain, double out[8]);
+/* out[0] total cells, out[1] resident blocks used, out[2] domains, out[3] largest n_sub. */
+int pf_batch_info(pf_batch *b, long long out[4]);
+/* Barrier wait limit; unreachable_barrier != 0 makes every group barrier wait
+ * for one block too many (to exercise the timeout path in tests). */
+int pf_batch_set_timeout(pf_batch *b, unsigned long long timeout_ns, int unreachable_barrier);
+int pf_batch_destroy(pf_batch *b);
+
 /* Reference output writers (write_data.cpp:3-82).  pf_write_data appends a
  * fraction_time.txt row under 'directory' when the reference would (or when
  * forced) and, if the model's micro_out flag is set, writes a VTI file. */

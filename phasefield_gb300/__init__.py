@@ -140,6 +140,14 @@ SYMBOLS = {
     "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
     "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
     "pf_reduce_noalloc": (_I, [ctypes.c_longlong, _I, _P, _P, _P, _P, _P, _P]),
+    "pf_batch_create": (_I, [ctypes.POINTER(PfModel), _I, ctypes.POINTER(_P)]),
+    "pf_batch_upload": (_I, [_P, _I, _P, _P, _P, _P, _D]),
+    "pf_batch_run": (_I, [_P, _I]),
+    "pf_batch_download": (_I, [_P, _I, _P, _P, _P, _P, _P, _DP]),
+    "pf_batch_reduce": (_I, [_P, _I, _DP]),
+    "pf_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
+    "pf_batch_set_timeout": (_I, [_P, ctypes.c_ulonglong, _I]),
+    "pf_batch_destroy": (_I, [_P]),
 }
 
 _lib = None
@@ -327,9 +335,62 @@ class PhaseField:
         check(lib().pf_kernel_times(self._ctx, t, n), "pf_kernel_times")
         return {"phase": (t[0], n[0]), "diffusion": (t[1], n[1])}
 
-    def write_data(self, directory: str | None = None, forced: bool = False) -> bool:
+    def write_data(self, directory: str | None = None, forced: bool = False) -> bool:  # noqa: D401
         """phase_field::Write_data (write_data.cpp:3-40)."""
         d = directory if directory is not None else self.model.directory.decode()
         w = ctypes.c_int()
         check(lib().pf_write_data(self._ctx, d.encode(), int(forced), ctypes.byref(w)), "pf_write_data")
         return bool(w.value)
+
+
+class Batch:
+    """Many independent 2D domains advanced by one persistent launch (pf_batch_*)."""
+
+    def __init__(self, models: list):
+        arr = (PfModel * len(models))(*models)
+        self.models = list(models)
+        self._b = ctypes.c_void_p()
+        check(lib().pf_batch_create(arr, len(models), ctypes.byref(self._b)), "pf_batch_create")
+
+    def close(self) -> None:
+        if self._b:
+            lib().pf_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, d: int, state: dict, time: float) -> None:
+        check(lib().pf_batch_upload(self._b, d, _ptr(state["ids"]), _ptr(state["phi"]), _ptr(state["phase"]),
+                                    _ptr(state["C"]), time), "pf_batch_upload")
+
+    def run(self, nsteps: int) -> int:
+        """Returns the status (PF_OK or PF_ERR_TIMEOUT) instead of raising on a timeout."""
+        st = lib().pf_batch_run(self._b, nsteps)
+        if st not in (PF_OK, PF_ERR_TIMEOUT):
+            check(st, "pf_batch_run")
+        return st
+
+    def download(self, d: int) -> dict:
+        st = empty_state(self.models[d])
+        t = ctypes.c_double()
+        check(lib().pf_batch_download(self._b, d, _ptr(st["ids"]), _ptr(st["phi"]), _ptr(st["phase"]),
+                                      _ptr(st["conc"]), _ptr(st["C"]), ctypes.byref(t)), "pf_batch_download")
+        st["time"] = t.value
+        return st
+
+    def reduce(self, d: int) -> np.ndarray:
+        out = np.zeros(8, np.float64)
+        check(lib().pf_batch_reduce(self._b, d, out.ctypes.data_as(_DP)), "pf_batch_reduce")
+        return out
+
+    def info(self) -> dict:
+        v = (ctypes.c_longlong * 4)()
+        check(lib().pf_batch_info(self._b, v), "pf_batch_info")
+        return {"cells": v[0], "blocks": v[1], "domains": v[2], "n_sub_max": v[3]}
+
+    def set_timeout(self, timeout_ns: int, unreachable_barrier: bool = False) -> None:
+        check(lib().pf_batch_set_timeout(self._b, timeout_ns, int(unreachable_barrier)), "pf_batch_set_timeout")

@@ -18,6 +18,7 @@ import concurrent.futures as cf
 import os
 import shutil
 import subprocess
+import sys
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
@@ -46,11 +47,13 @@ PER_FILE = {
     "pf_f64.cu": ["-fmad=false"],
     "pf_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "pf_f32_diffuse.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "pf_batch.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
              "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_reduce.cu", "pf_api.cu", "pf_reduce_noalloc.cu"]
+CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_batch.cu", "pf_reduce.cu", "pf_api.cu",
+              "pf_reduce_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
 HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h"]
 
@@ -97,7 +100,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, main, "-o", PFM, "-L", LIBDIR, "-lpfstep",
               "-Wl,-rpath,$ORIGIN/../lib"])
     if verbose:
-        print("built", LIB)
+        print("built", LIB, file=sys.stderr)
     return LIB
 
 

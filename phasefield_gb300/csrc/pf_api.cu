@@ -676,6 +676,245 @@ extern "C" int pf_use_graph(pf_ctx *c, int on) {
     return PF_OK;
 }
 
+// ===========================================================================
+// 3. Batched 2D domains: one persistent cooperative launch (pf_batch.cu).
+// ===========================================================================
+struct pf_batch {
+    std::vector<pf_ctx *> dom;
+    int nsol = 1;
+    cudaStream_t stream = nullptr;
+    pf_batch_dom *h_doms = nullptr, *d_doms = nullptr;
+    pf_f32_params *h_params = nullptr, *d_params = nullptr;
+    int *h_block_dom = nullptr, *d_block_dom = nullptr;
+    int max_blocks = 0, nblocks = 0;
+    unsigned long long *d_ctr = nullptr;
+    int *d_err = nullptr, *h_err = nullptr;
+    unsigned long long timeout_ns = 2000000000ull;  // 2 s per barrier wait
+    int extra_target = 0;
+    cudaGraphExec_t gexec = nullptr;
+    int g_steps = -1, g_blocks = -1;
+};
+
+namespace {
+void batch_free(pf_batch *b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (auto c : b->dom) pf_destroy(c);
+    cudaFree(b->d_doms); cudaFree(b->d_params); cudaFree(b->d_block_dom); cudaFree(b->d_ctr); cudaFree(b->d_err);
+    cudaFreeHost(b->h_doms); cudaFreeHost(b->h_params); cudaFreeHost(b->h_block_dom); cudaFreeHost(b->h_err);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+}  // namespace
+
+extern "C" int pf_batch_create(const pf_model *models, int ndom, pf_batch **out) {
+    if (!models || !out || ndom < 1) return pf_fail(PF_ERR_ARG, "pf_batch_create: bad arguments");
+    *out = nullptr;
+    for (int d = 0; d < ndom; d++) {
+        const pf_model &m = models[d];
+        if (m.iz != 1) return pf_fail(PF_ERR_ARG, "pf_batch_create: batched domains are 2D (iz == 1)");
+        if (m.nsol != models[0].nsol) return pf_fail(PF_ERR_ARG, "pf_batch_create: all domains need the same solutes");
+        for (int t = 1; t < m.nT; t++)
+            if (m.T_temp[t] != m.T_temp[0])
+                return pf_fail(PF_ERR_ARG, "pf_batch_create: each domain needs a constant temperature");
+    }
+    pf_batch *b = new pf_batch();
+    b->nsol = models[0].nsol;
+    int st = PF_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) st = pf_cuda_fail(e);
+    for (int d = 0; d < ndom && st == PF_OK; d++) {
+        pf_ctx *c = nullptr;
+        st = pf_create(&models[d], PF_PREC_FP32C, &c);
+        if (st == PF_OK) {
+            b->dom.push_back(c);
+            st = pf_set_stream(c, b->stream);
+        }
+    }
+    int dev = 0, sms = 0;
+    if (st == PF_OK) {
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        b->max_blocks = pf_batch_blocks_per_sm(b->nsol) * sms;
+        if (b->max_blocks < ndom) st = pf_fail(PF_ERR_RANGE, "pf_batch_create: more domains than resident blocks");
+    }
+    bool ok = st == PF_OK;
+    auto dalloc = [&](void **p, size_t n) { if (ok && cudaMalloc(p, n) != cudaSuccess) ok = false; };
+    auto halloc = [&](void **p, size_t n) { if (ok && cudaMallocHost(p, n) != cudaSuccess) ok = false; };
+    dalloc((void **)&b->d_doms, sizeof(pf_batch_dom) * ndom);
+    dalloc((void **)&b->d_params, sizeof(pf_f32_params) * ndom);
+    dalloc((void **)&b->d_block_dom, sizeof(int) * (b->max_blocks > 0 ? b->max_blocks : 1));
+    dalloc((void **)&b->d_ctr, sizeof(unsigned long long) * ndom);
+    dalloc((void **)&b->d_err, sizeof(int));
+    halloc((void **)&b->h_doms, sizeof(pf_batch_dom) * ndom);
+    halloc((void **)&b->h_params, sizeof(pf_f32_params) * ndom);
+    halloc((void **)&b->h_block_dom, sizeof(int) * (b->max_blocks > 0 ? b->max_blocks : 1));
+    halloc((void **)&b->h_err, sizeof(int));
+    if (st == PF_OK && !ok) {
+        cudaGetLastError();
+        st = pf_fail(PF_ERR_NOMEM, "pf_batch_create: allocation failed");
+    }
+    if (st != PF_OK) {
+        batch_free(b);
+        delete b;
+        return st;
+    }
+    *out = b;
+    return PF_OK;
+}
+
+extern "C" int pf_batch_destroy(pf_batch *b) {
+    if (!b) return PF_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
+    return PF_OK;
+}
+
+static int batch_dom_check(pf_batch *b, int d) {
+    if (!b || d < 0 || d >= (int)b->dom.size()) return pf_fail(PF_ERR_ARG, "pf_batch: bad domain index");
+    return PF_OK;
+}
+
+extern "C" int pf_batch_upload(pf_batch *b, int d, const int32_t *ids, const double *phi, const double *phase,
+                               const double *C, double time) {
+    int st = batch_dom_check(b, d);
+    if (st != PF_OK) return st;
+    if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+    return pf_upload_state(b->dom[d], ids, phi, phase, nullptr, C, time);
+}
+
+extern "C" int pf_batch_download(pf_batch *b, int d, int32_t *ids, double *phi, double *phase, double *conc,
+                                 double *C, double *time) {
+    int st = batch_dom_check(b, d);
+    if (st != PF_OK) return st;
+    return pf_download_state(b->dom[d], ids, phi, phase, conc, C, time);
+}
+
+extern "C" int pf_batch_reduce(pf_batch *b, int d, double out[8]) {
+    int st = batch_dom_check(b, d);
+    if (st != PF_OK) return st;
+    return pf_reduce(b->dom[d], out);
+}
+
+extern "C" int pf_batch_set_timeout(pf_batch *b, unsigned long long timeout_ns, int unreachable_barrier) {
+    if (!b) return pf_fail(PF_ERR_ARG, "pf_batch_set_timeout: null batch");
+    b->timeout_ns = timeout_ns;
+    b->extra_target = unreachable_barrier ? 1 : 0;
+    return PF_OK;
+}
+
+extern "C" int pf_batch_info(pf_batch *b, long long out[4]) {
+    if (!b || !out) return pf_fail(PF_ERR_ARG, "pf_batch_info: null argument");
+    long long cells = 0;
+    int nsub_max = 0;
+    for (auto c : b->dom) {
+        cells += c->N;
+        pf_step_params P;
+        pf_compute_params(c->model, c->time, P);
+        if (P.n_sub > nsub_max) nsub_max = P.n_sub;
+    }
+    out[0] = cells;
+    out[1] = b->nblocks > 0 ? b->nblocks : b->max_blocks;
+    out[2] = (long long)b->dom.size();
+    out[3] = nsub_max;
+    return PF_OK;
+}
+
+extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
+    if (!b || nsteps < 0) return pf_fail(PF_ERR_ARG, "pf_batch_run: bad arguments");
+    const int nd = (int)b->dom.size();
+    for (auto c : b->dom)
+        if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_batch_run: a domain has no state");
+    if (nsteps == 0) return PF_OK;
+    // Parameters, and block groups sized by work (phase sweep ~ 2 sub-steps).
+    const int tile = pf_batch_tile_cells();
+    std::vector<double> w(nd);
+    std::vector<int> tiles(nd), nsub(nd);
+    double wsum = 0.;
+    for (int d = 0; d < nd; d++) {
+        pf_ctx *c = b->dom[d];
+        pf_step_params P;
+        pf_compute_params(c->model, c->time, P);
+        pf_fold_f32(P, c->map.off[2], c->map.off[3], b->h_params[d]);
+        nsub[d] = P.n_sub;
+        const int tx = (c->model.ix + 31) / 32, ty = (c->model.iy + 7) / 8;
+        tiles[d] = tx * ty;
+        w[d] = (double)c->N * (2 + P.n_sub);
+        wsum += w[d];
+        b->h_doms[d].tiles_x = tx;
+        b->h_doms[d].tiles = tiles[d];
+    }
+    (void)tile;
+    std::vector<int> nb(nd);
+    int used = 0;
+    for (int d = 0; d < nd; d++) {
+        nb[d] = (int)((double)b->max_blocks * w[d] / wsum);
+        if (nb[d] < 1) nb[d] = 1;
+        if (nb[d] > tiles[d]) nb[d] = tiles[d];
+        used += nb[d];
+    }
+    while (used > b->max_blocks) {  // trim the largest groups
+        int big = 0;
+        for (int d = 1; d < nd; d++)
+            if (nb[d] > nb[big]) big = d;
+        nb[big]--;
+        used--;
+    }
+    int first = 0;
+    for (int d = 0; d < nd; d++) {
+        pf_ctx *c = b->dom[d];
+        pf_batch_dom &D = b->h_doms[d];
+        D.gid[0] = c->gid[0]; D.gid[1] = c->gid[1];
+        D.phi[0] = c->phi32[0]; D.phi[1] = c->phi32[1];
+        D.sph = c->phase32;
+        D.sol[0] = c->sol[0]; D.sol[1] = c->sol[1];
+        D.cur = c->cur; D.curs = c->curs;
+        D.nb_first = first;
+        D.nb = nb[d];
+        D.extra_target = b->extra_target;
+        for (int k = 0; k < nb[d]; k++) b->h_block_dom[first + k] = d;
+        first += nb[d];
+    }
+    b->nblocks = used;
+    // One graph per (steps, block count): the memcpy nodes read the pinned
+    // host tables at replay, so updated buffer roles and parameters flow in.
+    if (!b->gexec || b->g_steps != nsteps || b->g_blocks != used) {
+        if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+        cudaGraph_t g;
+        PF_CUDA_OK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaMemcpyAsync(b->d_doms, b->h_doms, sizeof(pf_batch_dom) * nd, cudaMemcpyHostToDevice, b->stream);
+        cudaMemcpyAsync(b->d_params, b->h_params, sizeof(pf_f32_params) * nd, cudaMemcpyHostToDevice, b->stream);
+        cudaMemcpyAsync(b->d_block_dom, b->h_block_dom, sizeof(int) * used, cudaMemcpyHostToDevice, b->stream);
+        cudaMemsetAsync(b->d_ctr, 0, sizeof(unsigned long long) * nd, b->stream);
+        cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
+        cudaError_t e1 = pf_launch_batch(b->nsol, used, b->d_doms, b->d_params, b->d_block_dom, nsteps, b->d_ctr,
+                                         b->d_err, b->timeout_ns, b->stream);
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) return pf_cuda_fail(e1 != cudaSuccess ? e1 : e2);
+        cudaError_t e3 = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) return pf_cuda_fail(e3);
+        b->g_steps = nsteps;
+        b->g_blocks = used;
+    }
+    PF_CUDA_OK(cudaGraphLaunch(b->gexec, b->stream));
+    PF_CUDA_OK(cudaMemcpyAsync(b->h_err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    PF_CUDA_OK(cudaStreamSynchronize(b->stream));
+    if (*b->h_err) return pf_fail(PF_ERR_TIMEOUT, "pf_batch_run: a domain barrier timed out; the launch was abandoned");
+    for (int d = 0; d < nd; d++) {
+        pf_ctx *c = b->dom[d];
+        c->cur ^= (nsteps & 1);
+        c->curs ^= ((long long)nsteps * nsub[d]) & 1;
+        pf_step_params P;
+        for (int s = 0; s < nsteps; s++) {  // the same time accumulation as pf_step
+            pf_compute_params(c->model, c->time, P);
+            c->time += P.pfm_dt;
+        }
+        c->last = P;
+        c->have_last = true;
+    }
+    return PF_OK;
+}
+
 extern "C" int pf_write_data(pf_ctx *c, const char *directory, int forced, int *written) {
     if (!c || !directory) return pf_fail(PF_ERR_ARG, "pf_write_data: null argument");
     if (written) *written = 0;

@@ -28,156 +28,13 @@ __global__ void __launch_bounds__(kPT) k_phase_f32(const __grid_constant__ pf_f3
                                                    ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
                                                    float *__restrict__ sphase,
                                                    const float2 *__restrict__ sol) {
-    __shared__ int s_id[PF_NSTENCIL][kPT];
-    __shared__ float s_v1[PF_NSTENCIL][kPT];   // own phi of the entry (0 if only a neighbour has it)
-    __shared__ float s_v2[PF_NSTENCIL][kPT];   // sum of the neighbours' phi of the entry
-    __shared__ float s_del[PF_NSTENCIL][kPT];  // increment, then the updated value
+    __shared__ pf_plist<kPT> L;
     const int t = threadIdx.x + kPX * threadIdx.y;
     const int i = blockIdx.x * kPX + threadIdx.x;
     const int j = blockIdx.y * kPY + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= P.ix || j >= P.iy) return;
-    const int ix = P.ix, iy = P.iy, iz = P.iz;
-    const long long plane = (long long)ix * iy;
-    const long long n = i + (long long)ix * j + plane * k;
-    const float cutoff = P.cutoff;
-    const int b1 = P.b1, b2 = P.b2;
-
-    const ushort4 g = __ldg(gid1 + n);
-    const float4 v = __ldg(phi1 + n);
-    const int oid[4] = {g.x, g.y, g.z, g.w};
-    const float ov[4] = {v.x, v.y, v.z, v.w};
-    // solver.cpp:168-177: own slots above the cutoff (a sorted prefix).
-    int num = 0;
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        if (ov[a] > cutoff) {
-            s_id[num][t] = oid[a];
-            s_v1[num][t] = ov[a];
-            s_v2[num][t] = 0.f;
-            num++;
-        }
-    }
-    // solver.cpp:179-205: merge the neighbours' lists (x-, x+, y-, y+, z-, z+),
-    // each scanned until its first empty slot.
-    long long nb[6];
-    nb[0] = n - i + pf_wrap(i, ix, -1);
-    nb[1] = n - i + pf_wrap(i, ix, 1);
-    nb[2] = n + (long long)ix * (pf_wrap(j, iy, -1) - j);
-    nb[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
-    nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
-    nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
-#pragma unroll
-    for (int b = 0; b < 6; b++) {
-        if (b < P.nnb) {
-            const ushort4 ng = __ldg(gid1 + nb[b]);
-            const float4 nv4 = __ldg(phi1 + nb[b]);
-            const int nid[4] = {ng.x, ng.y, ng.z, ng.w};
-            const float nv[4] = {nv4.x, nv4.y, nv4.z, nv4.w};
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                const int tid = nid[a];
-                if (tid == 0) break;
-                int kk = 0;
-                while (kk < num && s_id[kk][t] != tid) kk++;
-                if (kk < num) {
-                    s_v2[kk][t] += nv[a];
-                } else if (num < PF_NSTENCIL) {
-                    s_id[num][t] = tid;
-                    s_v1[num][t] = 0.f;
-                    s_v2[num][t] = nv[a];
-                    num++;
-                }
-            }
-        }
-    }
-    if (num == 1) {  // solver.cpp:207-216: bulk, copy and leave the phase planes untouched
-        gid2[n] = g;
-        phi2[n] = v;
-        return;
-    }
-    // Carbon concentration of each phase in this cell (for the driving force),
-    // partitioned with the phase fractions of the current slots.
-    float ph_old[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        const int p = pf_lphase(oid[a], b1, b2);
-        if (p == 1) ph_old[0] += ov[a];
-        else if (p == 2) ph_old[1] += ov[a];
-        else if (p == 3) ph_old[2] += ov[a];
-    }
-    float lc[3];
-    pf_partition_q(P, 0, __ldg(sol + n * NSOL).x, ph_old, lc);
-
-    // Pair terms (solver.cpp:235-258), each unordered pair once:
-    //   X = S_i phi_j - S_j phi_i and Y = phi_i - phi_j flip sign between (i,j)
-    //   and (j,i), Z = sqrt(phi_i phi_j) does not; A, B are symmetric in the
-    //   phase pair, G and E are not.  A = B = G = 0 for pairs that do not interact.
-    for (int a = 0; a < num; a++) s_del[a][t] = 0.f;
-    for (int a = 0; a < num; a++) {
-        const int ia = s_id[a][t];
-        const int pa = pf_lphase(ia, b1, b2);
-        const float va1 = s_v1[a][t], va2 = s_v2[a][t];
-        const float ca = pa == 1 ? lc[0] : (pa == 2 ? lc[1] : lc[2]);
-        float da = s_del[a][t];
-        for (int b = a + 1; b < num; b++) {
-            const int pb = pf_lphase(s_id[b][t], b1, b2);
-            const float vb1 = s_v1[b][t], vb2 = s_v2[b][t];
-            const int e = (pa - 1) + 3 * (pb - 1), ee = (pb - 1) + 3 * (pa - 1);
-            const float X = va2 * vb1 - vb2 * va1;
-            const float Y = va1 - vb1;
-            const float Z = sqrtf(va1 * vb1);
-            const float sym = P.A[e] * X + P.B[e] * Y;
-            const float cb = pb == 1 ? lc[0] : (pb == 2 ? lc[1] : lc[2]);
-            da += sym + P.G[e] * Z * (ca - P.E[e]);
-            s_del[b][t] += -sym + P.G[ee] * Z * (cb - P.E[ee]);
-        }
-        float d = va1 + da;
-        if (d > 1.0f) d = 1.0f;
-        else if (d < cutoff) d = 0.f;
-        s_del[a][t] = d;
-    }
-    // Top four, first maximum wins (solver.cpp:426-432), keep > cutoff,
-    // normalise with x * (1/sum) (solver.cpp:276-296).
-    float ph[3] = {0.f, 0.f, 0.f};
-    float sum = 0.f;
-    int kid[4];
-    float kv[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-        kid[a] = 0;
-        kv[a] = 0.f;
-        if (a < num) {
-            int mx = a;
-            float mv = s_del[a][t];
-            for (int b = a + 1; b < num; b++) {
-                const float x = s_del[b][t];
-                if (x > mv) { mv = x; mx = b; }
-            }
-            const int mid = s_id[mx][t];
-            if (mx != a) {
-                s_del[mx][t] = s_del[a][t];
-                s_id[mx][t] = s_id[a][t];
-            }
-            if (mv > cutoff) {
-                kid[a] = mid;
-                kv[a] = mv;
-                const int p = pf_lphase(mid, b1, b2);
-                if (p == 1) ph[0] += mv;
-                else if (p == 2) ph[1] += mv;
-                else ph[2] += mv;
-                sum += mv;
-            }
-        }
-    }
-    const float inv = 1.f / sum;
-    gid2[n] = make_ushort4((unsigned short)kid[0], (unsigned short)kid[1], (unsigned short)kid[2],
-                           (unsigned short)kid[3]);
-    phi2[n] = make_float4(kv[0] * inv, kv[1] * inv, kv[2] * inv, kv[3] * inv);
-    const long long N = P.N;
-    sphase[n] = sqrtf(ph[0] * inv);
-    sphase[N + n] = sqrtf(ph[1] * inv);
-    sphase[2 * N + n] = sqrtf(ph[2] * inv);
+    pf_phase_cell<NSOL, kPT>(P, i, j, k, t, gid1, phi1, gid2, phi2, sphase, sol, L);
 }
 
 // Per-class maximum of (id mod 100000) over all slots, for the local id map.

@@ -45,6 +45,23 @@ int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max);
 cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, const float2 *sol_in,
                                   float2 *sol_out, cudaStream_t s, const pf_diff_cfg *cfg);
 
+// ---- batched 2D domains, one persistent cooperative launch (pf_batch.cu) ----
+struct pf_batch_dom {
+    ushort4 *gid[2];
+    float4 *phi[2];
+    float *sph;
+    float2 *sol[2];
+    int cur, curs;          // buffer roles at the start of the launch
+    int nb_first, nb;       // the domain's block group
+    int tiles_x, tiles;     // 32x8 tiles of the domain
+    int extra_target;       // test knob: > 0 makes the group barriers unreachable
+};
+int pf_batch_blocks_per_sm(int nsol);
+int pf_batch_tile_cells();
+cudaError_t pf_launch_batch(int nsol, int nblocks, const pf_batch_dom *doms, const pf_f32_params *params,
+                            const int *block_dom, int nsteps, unsigned long long *ctr, int *err,
+                            unsigned long long timeout_ns, cudaStream_t s);
+
 // ---- FP64 reductions (pf_reduce.cu) ----
 // out[0..2]  sum of phase fractions, out[3] sum of phi over slots whose grain
 // id is below 100000 (write_data.cpp:18), out[4..5] solute sums, out[6]

@@ -187,3 +187,57 @@ WORKLOADS = {
 
 def packaged_config(name: str) -> str:
     return os.path.join(CONFIG_DIR, f"{name}.txt")
+
+
+@dataclass
+class EnsembleDomain:
+    grid: tuple
+    T: float
+    C0: float
+    n_grains: int
+    n_nuclei: int
+    seed: int
+
+
+def ensemble(n_domains: int = 64, seed: int = 0, sizes=(128, 512), T_range=(993.0, 1053.0),
+             C_range=(0.05, 0.20)) -> list:
+    """The batched ensemble: square 2D domains with sides drawn uniform from the
+    multiples of 32 in [sizes], temperature and carbon drawn uniform from the
+    ranges, and per-domain grain and nucleus densities, all from one seed."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sides = np.arange(sizes[0], sizes[1] + 1, 32)
+    out = []
+    for d in range(n_domains):
+        L = int(rng.choice(sides))
+        T = float(rng.uniform(*T_range))
+        C0 = float(rng.uniform(*C_range))
+        grains = max(2, int(round(L * L / float(rng.uniform(2000.0, 6000.0)))))
+        nuclei = int(round(L * L * float(rng.uniform(2e-4, 8e-4))))
+        out.append(EnsembleDomain((L, L, 1), T, C0, grains, nuclei, int(seed * 1000 + d)))
+    return out
+
+
+def ensemble_inputs(directory: str, domains: list) -> list:
+    """Write one config file per ensemble domain; returns their paths."""
+    os.makedirs(directory, exist_ok=True)
+    write_thermo(os.path.join(directory, "thermo_steel.txt"))
+    paths = []
+    for d, dom in enumerate(domains):
+        paths.append(write_config(os.path.join(directory, f"ens{d:03d}.txt"), grid=dom.grid, T=dom.T,
+                                  num_grain=(dom.n_grains, 0, 0), num_nuclei=dom.n_nuclei,
+                                  directory=os.path.join(directory, f"out{d:03d}")))
+    return paths
+
+
+def ensemble_spec(dom: EnsembleDomain) -> PfInitSpec:
+    s = PfInitSpec()
+    s.seed = dom.seed
+    s.n_grains = dom.n_grains
+    s.n_nuclei = dom.n_nuclei
+    s.nucleus_radius = 3.0
+    s.width = 6.0
+    s.C0[0], s.C0[1] = dom.C0, 1.5
+    s.max_slots = 4
+    return s
