@@ -363,6 +363,17 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
                "sample": label + f", {nst} steps"}
 
     ms_step = ms / args.steps
+    # DRAM traffic of the diffusion kernel: bytes per cell from the committed ncu
+    # capture of a 256x256x64 case (profiles/ncu_traffic.json), scaled to this
+    # launch by its cell count.
+    traffic, traffic_src = None, None
+    tpath = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f).get("k_diffuse")
+        if tj:
+            traffic = tj["dram_bytes_per_cell"] * N
+            traffic_src = f"ncu dram__bytes_read+write on {tj['case']}, scaled by cell count"
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -375,7 +386,8 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
                    "l2": f"inputs larger than L2 (FP32 state {N * 52 / 1e9:.2f} GB, L2 0.13 GB)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None, "kernel": "k_diffuse_f32",
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": "k_diffuse_f32",
                      "algorithmic_bytes_per_launch": diff_bytes, "mean_launch_ms": t_diff * 1e3,
                      "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)"},
         "kernels": {
