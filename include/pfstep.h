@@ -223,6 +223,29 @@ int pf_batch_info(pf_batch *b, long long out[4]);
 int pf_batch_set_timeout(pf_batch *b, unsigned long long timeout_ns, int unreachable_barrier);
 int pf_batch_destroy(pf_batch *b);
 
+/* Adjoint of the explicit step (no reference counterpart), for calibration.
+ * The calibration model is the four-slot compact step (carbon only: Mn does
+ * not enter the phase update or the carbon field), in FP64 (PF_PREC_FP64) or
+ * FP32 with FP64 reductions (PF_PREC_FP32C).  Parameters are scale factors
+ * s[4] on the interface mobilities, the interface energies, D_C and D_Mn; the
+ * time step and sub-step count are those of s = 1 and stay fixed.
+ * pf_adj_forward runs nsteps from the uploaded state, keeping a checkpoint
+ * every checkpoint_every steps, and returns J[0] = mean ferrite fraction and
+ * J[1] = mean austenite carbon (sum phi_2 c_2 / sum phi_2) at the end.
+ * pf_adj_gradient(objective 0 or 1) then returns dJ/ds by the hand-written
+ * reverse sweep (segments recomputed from the checkpoints, discrete decisions
+ * of every step held fixed).  pf_adj_timings: ms of the last forward and of
+ * the last gradient (recomputation included). */
+typedef struct pf_adj pf_adj;
+int pf_adj_create(const pf_model *model, int precision, int checkpoint_every, pf_adj **out);
+int pf_adj_upload(pf_adj *a, const int32_t *ids, const double *phi, const double *phase, const double *C,
+                  double time);
+int pf_adj_set_scales(pf_adj *a, const double scales[4]);
+int pf_adj_forward(pf_adj *a, int nsteps, double J[2]);
+int pf_adj_gradient(pf_adj *a, int objective, double grad[4]);
+int pf_adj_timings(pf_adj *a, double ms[2]);
+int pf_adj_destroy(pf_adj *a);
+
 /* Reference output writers (write_data.cpp:3-82).  pf_write_data appends a
  * fraction_time.txt row under 'directory' when the reference would (or when
  * forced) and, if the model's micro_out flag is set, writes a VTI file. */

@@ -148,6 +148,13 @@ SYMBOLS = {
     "pf_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     "pf_batch_set_timeout": (_I, [_P, ctypes.c_ulonglong, _I]),
     "pf_batch_destroy": (_I, [_P]),
+    "pf_adj_create": (_I, [ctypes.POINTER(PfModel), _I, _I, ctypes.POINTER(_P)]),
+    "pf_adj_upload": (_I, [_P, _P, _P, _P, _P, _D]),
+    "pf_adj_set_scales": (_I, [_P, _DP]),
+    "pf_adj_forward": (_I, [_P, _I, _DP]),
+    "pf_adj_gradient": (_I, [_P, _I, _DP]),
+    "pf_adj_timings": (_I, [_P, _DP]),
+    "pf_adj_destroy": (_I, [_P]),
 }
 
 _lib = None
@@ -394,3 +401,47 @@ class Batch:
 
     def set_timeout(self, timeout_ns: int, unreachable_barrier: bool = False) -> None:
         check(lib().pf_batch_set_timeout(self._b, timeout_ns, int(unreachable_barrier)), "pf_batch_set_timeout")
+
+
+class Adjoint:
+    """Forward + hand-written adjoint of the compact step (pf_adj_*)."""
+
+    def __init__(self, model: PfModel, precision: int = PF_PREC_FP64, checkpoint_every: int = 100):
+        self.model = model
+        self._a = ctypes.c_void_p()
+        check(lib().pf_adj_create(ctypes.byref(model), precision, checkpoint_every, ctypes.byref(self._a)),
+              "pf_adj_create")
+
+    def close(self) -> None:
+        if self._a:
+            lib().pf_adj_destroy(self._a)
+            self._a = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, state: dict, time: float) -> None:
+        check(lib().pf_adj_upload(self._a, _ptr(state["ids"]), _ptr(state["phi"]), _ptr(state["phase"]),
+                                  _ptr(state["C"]), time), "pf_adj_upload")
+
+    def set_scales(self, scales) -> None:
+        s = np.ascontiguousarray(scales, np.float64)
+        check(lib().pf_adj_set_scales(self._a, s.ctypes.data_as(_DP)), "pf_adj_set_scales")
+
+    def forward(self, nsteps: int) -> np.ndarray:
+        J = np.zeros(2, np.float64)
+        check(lib().pf_adj_forward(self._a, nsteps, J.ctypes.data_as(_DP)), "pf_adj_forward")
+        return J
+
+    def gradient(self, objective: int) -> np.ndarray:
+        g = np.zeros(4, np.float64)
+        check(lib().pf_adj_gradient(self._a, objective, g.ctypes.data_as(_DP)), "pf_adj_gradient")
+        return g
+
+    def timings(self) -> dict:
+        t = np.zeros(2, np.float64)
+        check(lib().pf_adj_timings(self._a, t.ctypes.data_as(_DP)), "pf_adj_timings")
+        return {"forward_ms": float(t[0]), "gradient_ms": float(t[1])}

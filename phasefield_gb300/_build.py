@@ -48,12 +48,13 @@ PER_FILE = {
     "pf_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "pf_f32_diffuse.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "pf_batch.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "pf_adjoint.cu": ["-fmad=false"],
 }
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
              "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_batch.cu", "pf_reduce.cu", "pf_api.cu",
-              "pf_reduce_noalloc.cu"]
+              "pf_reduce_noalloc.cu", "pf_adjoint.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
 HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h"]
 

@@ -1,0 +1,847 @@
+// pf_adjoint.cu -- hand-written adjoint of the explicit time step (sm_103a).
+//
+// The calibration model is the compact four-slot step of the FP32 path
+// (Phase_field_solver, solver.cpp:147-304, and the multiphase carbon diffusion
+// with partitioning, solver.cpp:343-405), written here once for a real type R
+// so that it runs in FP64 (the finite-difference reference) and in FP32 with
+// FP64 reductions.  State per cell: 4 local grain ids, their phi, the 3 phase
+// fractions, the total carbon.  (Mn does not enter the phase update or the
+// carbon diffusion, so the gradients below do not depend on it.)
+//
+// Parameters: scale factors s = (mobility, interface energy, D_C, D_Mn) on
+// m_ij, sigma_ij, D_C,p, D_Mn,p.  The time step and the sub-step count are
+// those of s = 1 and are held fixed, so the step is a smooth function of s
+// between discrete events.
+//
+// Objectives at the final time:  J0 = mean ferrite fraction (1/N) sum phi_1,
+// J1 = mean austenite carbon  sum phi_2 c_2 / sum phi_2.
+//
+// Adjoint: the discrete decisions of every step (stencil list membership, the
+// cutoff and unit clamps, the top-four choice) are recomputed from the stored
+// pre-step state with the same code as the forward step and held fixed.  With
+// lambda the adjoint of the state after a sweep:
+// * diffusion sub-step (linear in C for fixed phase fractions):
+//     lam_C(m) = lam(m) + sum_p D_p s_p(m)/t1_p(m) sum_nb s_p(nb) (lam(nb) - lam(m))
+//   (the same stencil as the flux, with lambda in place of c), plus the
+//   phase-fraction adjoint from s_p = sqrt(phi_p) and c_p(phi);
+// * phase sweep: the normalisation and the pair terms are differentiated per
+//   cell; the neighbour sums S_e = sum_nb phi_nb(e) are returned to the
+//   neighbours' slots by a gather over the neighbours' published lists.
+// Checkpoints every K steps; a segment is recomputed forward storing every
+// step's pre-step state and pre-sub-step carbon, then swept backwards.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "pf_dev.cuh"
+#include "pf_host.h"
+#include "pf_kernels.h"
+
+namespace {
+
+constexpr int LMAX = PF_NSTENCIL;
+
+template <typename R>
+struct AP {
+    int ix, iy, iz, nnb, n_sub, b1, b2;
+    long long N;
+    R cutoff;
+    R A[9], B[9], G[9], E[9];  // dt*m*sigma*f1, dt*m*sigma*f2, dt*m*f3*entropy/dcdT, eq  (scaled)
+    R D[3];                    // D_C,p * dt_sub/dx^2 (scaled)
+    R k[9], c[9];              // carbon partition
+    R s_m, s_s, s_c;           // the scales (for gradients of scaled terms)
+};
+
+__device__ __forceinline__ int lphase(int l, int b1, int b2) { return l == 0 ? 0 : (l <= b1 ? 1 : (l <= b2 ? 2 : 3)); }
+
+__device__ __forceinline__ void neighbours(long long n, int ix, int iy, int iz, long long nb[6]) { pf_neighbours(n, ix, iy, iz, nb); }
+
+template <typename R>
+__device__ __forceinline__ void partition(const AP<R> &P, R C, const R ph[3], R c[3], R t1[3]) {
+    for (int i = 0; i < 3; i++) {
+        R a = 0, b = 0;
+        for (int j = 0; j < 3; j++) {
+            a += ph[j] * P.k[i + 3 * j];
+            b += ph[j] * P.c[i + 3 * j];
+        }
+        t1[i] = a;
+        c[i] = (C - b) / a;
+    }
+}
+
+// The per-cell stencil list of the phase sweep, with every decision.
+template <typename R>
+struct Lst {
+    int num, bulk, kept;
+    int id[LMAX], pe[LMAX], own[LMAX];
+    R v1[LMAX], S[LMAX], draw[LMAX], d[LMAX];
+    int perm[4];
+    R sum;
+    int oid[4];
+    R ov[4];
+    R ph_old[3], c[3], t1[3];
+};
+
+template <typename R>
+__device__ void build_list(const AP<R> &P, long long n, const ushort4 *gid, const R *phi, const R *C, Lst<R> &L) {
+    long long nb[6];
+    neighbours(n, P.ix, P.iy, P.iz, nb);
+    const ushort4 g = gid[n];
+    L.oid[0] = g.x; L.oid[1] = g.y; L.oid[2] = g.z; L.oid[3] = g.w;
+    for (int a = 0; a < 4; a++) L.ov[a] = phi[4 * n + a];
+    int num = 0;
+    for (int a = 0; a < 4; a++)
+        if (L.ov[a] > P.cutoff) {
+            L.id[num] = L.oid[a]; L.v1[num] = L.ov[a]; L.S[num] = 0; L.own[num] = a;
+            num++;
+        }
+    for (int b = 0; b < P.nnb; b++) {
+        const long long m = nb[b];
+        const ushort4 q = gid[m];
+        const int qid[4] = {q.x, q.y, q.z, q.w};
+        for (int a = 0; a < 4; a++) {
+            const int t = qid[a];
+            if (t == 0) break;
+            const R v = phi[4 * m + a];
+            int kk = 0;
+            while (kk < num && L.id[kk] != t) kk++;
+            if (kk < num) L.S[kk] += v;
+            else if (num < LMAX) {
+                L.id[num] = t; L.v1[num] = 0; L.S[num] = v; L.own[num] = -1;
+                num++;
+            }
+        }
+    }
+    L.num = num;
+    L.bulk = (num == 1);
+    for (int e = 0; e < num; e++) L.pe[e] = lphase(L.id[e], P.b1, P.b2);
+    for (int p = 0; p < 3; p++) L.ph_old[p] = 0;
+    for (int a = 0; a < 4; a++) {
+        const int p = lphase(L.oid[a], P.b1, P.b2);
+        if (p > 0) L.ph_old[p - 1] += L.ov[a];
+    }
+    partition(P, C[n], L.ph_old, L.c, L.t1);
+    if (L.bulk) return;
+    for (int e = 0; e < num; e++) {
+        R acc = 0;
+        const int pe = L.pe[e];
+        for (int f = 0; f < num; f++) {
+            if (f == e) continue;
+            const int x = (pe - 1) + 3 * (L.pe[f] - 1);
+            const R X = L.S[e] * L.v1[f] - L.S[f] * L.v1[e];
+            const R Y = L.v1[e] - L.v1[f];
+            const R Z = sqrt(L.v1[e] * L.v1[f]);
+            acc += P.A[x] * X + P.B[x] * Y + P.G[x] * Z * (L.c[pe - 1] - P.E[x]);
+        }
+        const R dr = L.v1[e] + acc;
+        L.draw[e] = dr;
+        L.d[e] = dr > (R)1 ? (R)1 : (dr < P.cutoff ? (R)0 : dr);
+    }
+    // Top four, first maximum wins (solver.cpp:426-432).
+    int idx[LMAX];
+    for (int e = 0; e < num; e++) idx[e] = e;
+    L.kept = 0;
+    L.sum = 0;
+    for (int a = 0; a < 4; a++) {
+        L.perm[a] = -1;
+        if (a >= num) continue;
+        int mx = a;
+        for (int b = a + 1; b < num; b++)
+            if (L.d[idx[b]] > L.d[idx[mx]]) mx = b;
+        const int t = idx[a]; idx[a] = idx[mx]; idx[mx] = t;
+        if (L.d[idx[a]] > P.cutoff) {
+            L.perm[a] = idx[a];
+            L.kept++;
+            L.sum += L.d[idx[a]];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- forward --
+template <typename R>
+__global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
+                            R *phi2, R *ph2) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    Lst<R> L;
+    build_list(P, n, gid, phi, C, L);
+    if (L.bulk) {
+        gid2[n] = gid[n];
+        for (int a = 0; a < 4; a++) phi2[4 * n + a] = phi[4 * n + a];
+        for (int p = 0; p < 3; p++) ph2[3 * n + p] = ph[3 * n + p];
+        return;
+    }
+    const R inv = (R)1 / L.sum;
+    int oid[4] = {0, 0, 0, 0};
+    R q[3] = {0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+        R v = 0;
+        if (L.perm[a] >= 0) {
+            const int e = L.perm[a];
+            oid[a] = L.id[e];
+            v = L.d[e] * inv;
+            q[L.pe[e] - 1] += L.d[e];
+        }
+        phi2[4 * n + a] = v;
+    }
+    gid2[n] = make_ushort4((unsigned short)oid[0], (unsigned short)oid[1], (unsigned short)oid[2], (unsigned short)oid[3]);
+    for (int p = 0; p < 3; p++) ph2[3 * n + p] = q[p] * inv;
+}
+
+// Flux of one cell (the forward sub-step's increment), neighbours partitioned on the fly.
+template <typename R>
+__device__ R flux_at(const AP<R> &P, long long n, const R *ph, const R *C) {
+    long long nb[6];
+    neighbours(n, P.ix, P.iy, P.iz, nb);
+    const R p0[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+    R c0[3], t0[3];
+    partition(P, C[n], p0, c0, t0);
+    R f = 0;
+    for (int p = 0; p < 3; p++) {
+        const R s0 = sqrt(p0[p]);
+        R a = 0;
+        for (int b = 0; b < P.nnb; b++) {
+            const long long m = nb[b];
+            const R pm[3] = {ph[3 * m], ph[3 * m + 1], ph[3 * m + 2]};
+            R cm[3], tm[3];
+            partition(P, C[m], pm, cm, tm);
+            a += sqrt(pm[p]) * (cm[p] - c0[p]);
+        }
+        f += s0 * P.D[p] * a;
+    }
+    return f;
+}
+
+template <typename R>
+__global__ void k_fwd_diffuse(const AP<R> P, const R *ph, const R *C, R *C2) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    C2[n] = C[n] + flux_at(P, n, ph, C);
+}
+
+// Objective sums in FP64: out[0] = sum phi_1, out[1] = sum phi_2, out[2] = sum phi_2 c_2.
+template <typename R>
+__global__ void k_objective_sums(const AP<R> P, const R *ph, const R *C, double *out) {
+    double a = 0, b = 0, cc = 0;
+    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < P.N; n += (long long)gridDim.x * blockDim.x) {
+        const R p[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+        R c[3], t[3];
+        partition(P, C[n], p, c, t);
+        a += (double)p[0];
+        b += (double)p[1];
+        cc += (double)p[1] * (double)c[1];
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, s);
+        b += __shfl_down_sync(0xffffffffu, b, s);
+        cc += __shfl_down_sync(0xffffffffu, cc, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, a);
+        atomicAdd(out + 1, b);
+        atomicAdd(out + 2, cc);
+    }
+}
+
+// ---------------------------------------------------------------- adjoint --
+// Seed at the final state.  obj 0: J = sum phi_1 / N.  obj 1: J = sum phi_2 c_2 / W.
+template <typename R>
+__global__ void k_seed(const AP<R> P, int obj, const R *ph, const R *C, double W, double J, R *lph, R *lC, R *lphi) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    for (int a = 0; a < 4; a++) lphi[4 * n + a] = 0;
+    if (obj == 0) {
+        lph[3 * n] = (R)(1.0 / (double)P.N);
+        lph[3 * n + 1] = 0;
+        lph[3 * n + 2] = 0;
+        lC[n] = 0;
+        return;
+    }
+    const R p[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+    R c[3], t[3];
+    partition(P, C[n], p, c, t);
+    const R iw = (R)(1.0 / W);
+    lC[n] = p[1] / t[1] * iw;
+    for (int j = 0; j < 3; j++) {
+        const R dc = -(P.c[1 + 3 * j] + c[1] * P.k[1 + 3 * j]) / t[1];  // dc_2/dphi_j
+        R v = p[1] * dc;
+        if (j == 1) v += c[1] - (R)J;
+        lph[3 * n + j] = v * iw;
+    }
+}
+
+// Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
+// sub-step), C (before it), ph.  Out: lam2 (adjoint of C before), lph += the
+// phase-fraction part, grad[2] += dJ/ds_C.
+template <typename R>
+__global__ void k_bwd_diffuse(const AP<R> P, const R *ph, const R *C, const R *lam, R *lam2, R *lph, double *grad) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double g = 0;
+    if (n < P.N) {
+        long long nb[6];
+        neighbours(n, P.ix, P.iy, P.iz, nb);
+        const R p0[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+        R c0[3], t0[3];
+        partition(P, C[n], p0, c0, t0);
+        const R l0 = lam[n];
+        R out = l0;
+        R dL_ds[3] = {0, 0, 0}, dL_dc[3] = {0, 0, 0};
+        R flux = 0;
+        for (int p = 0; p < 3; p++) {
+            const R s0 = sqrt(p0[p]);
+            R al = 0, ac = 0, ads = 0;
+            for (int b = 0; b < P.nnb; b++) {
+                const long long m = nb[b];
+                const R pm[3] = {ph[3 * m], ph[3 * m + 1], ph[3 * m + 2]};
+                R cm[3], tm[3];
+                partition(P, C[m], pm, cm, tm);
+                const R sm = sqrt(pm[p]);
+                al += sm * (lam[m] - l0);
+                ac += sm * (cm[p] - c0[p]);
+                ads += sm * (cm[p] - c0[p]) * (l0 - lam[m]);
+            }
+            out += P.D[p] * s0 / t0[p] * al;
+            dL_dc[p] = P.D[p] * s0 * al;
+            dL_ds[p] = P.D[p] * ads;
+            flux += s0 * P.D[p] * ac;
+        }
+        lam2[n] = out;
+        for (int j = 0; j < 3; j++) {
+            R v = 0;
+            for (int p = 0; p < 3; p++) v += dL_dc[p] * (-(P.c[p + 3 * j] + c0[p] * P.k[p + 3 * j]) / t0[p]);
+            if (p0[j] > 0) v += dL_ds[j] / ((R)2 * sqrt(p0[j]));
+            lph[3 * n + j] += v;
+        }
+        g = (double)l0 * (double)flux / (double)P.s_c;
+    }
+    for (int s = 16; s > 0; s >>= 1) g += __shfl_down_sync(0xffffffffu, g, s);
+    if ((threadIdx.x & 31) == 0 && g != 0) atomicAdd(grad + 2, g);
+}
+
+// Reverse of the phase sweep, own-cell part.  In: pre-step state, lam_phi /
+// lam_ph of the post-sweep state, lam_C (adjoint of C after the sweep, which
+// the sweep does not change).  Out: lam_phi_pre (own part), lam_ph_pre,
+// lam_C += driving-force part, the published neighbour-sum adjoints (ids, lS),
+// grad[0..1] += dJ/ds_m, dJ/ds_sigma.
+template <typename R>
+__global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph_pre, const R *C,
+                                const R *lphi_post, const R *lph_post, R *lC, R *lphi_pre, R *lph_pre, int *pub_id,
+                                R *pub_l, double *grad) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double gm = 0, gs = 0;
+    if (n < P.N) {
+        Lst<R> L;
+        build_list(P, n, gid, phi, C, L);
+        for (int e = 0; e < LMAX; e++) pub_id[LMAX * n + e] = 0;
+        if (L.bulk) {
+            for (int a = 0; a < 4; a++) lphi_pre[4 * n + a] = lphi_post[4 * n + a];
+            for (int p = 0; p < 3; p++) lph_pre[3 * n + p] = lph_post[3 * n + p];
+        } else {
+            for (int p = 0; p < 3; p++) lph_pre[3 * n + p] = 0;
+            // Normalisation: phi'_a = d_perm(a)/D, ph'_p = sum_{a in p} d/D.
+            const R D = L.sum, inv = (R)1 / D;
+            R mu = 0;
+            for (int a = 0; a < 4; a++)
+                if (L.perm[a] >= 0) {
+                    const int e = L.perm[a];
+                    mu += lphi_post[4 * n + a] * L.d[e] * inv;
+                }
+            R q[3] = {0, 0, 0};
+            for (int a = 0; a < 4; a++)
+                if (L.perm[a] >= 0) q[L.pe[L.perm[a]] - 1] += L.d[L.perm[a]];
+            for (int p = 0; p < 3; p++) mu += lph_post[3 * n + p] * q[p] * inv;
+            mu *= inv;
+            R ld[LMAX];
+            for (int e = 0; e < L.num; e++) ld[e] = 0;
+            for (int a = 0; a < 4; a++)
+                if (L.perm[a] >= 0) {
+                    const int e = L.perm[a];
+                    ld[e] = (lphi_post[4 * n + a] + lph_post[3 * n + L.pe[e] - 1]) * inv - mu;
+                }
+            // Clamps: only values strictly inside [cutoff, 1] carry a derivative.
+            for (int e = 0; e < L.num; e++)
+                if (L.draw[e] > (R)1 || L.draw[e] < P.cutoff) ld[e] = 0;
+            // Pair terms.
+            R lv1[LMAX], lS[LMAX], lc[3] = {0, 0, 0};
+            for (int e = 0; e < L.num; e++) { lv1[e] = ld[e]; lS[e] = 0; }
+            for (int e = 0; e < L.num; e++) {
+                if (ld[e] == (R)0) continue;
+                const int pe = L.pe[e];
+                for (int f = 0; f < L.num; f++) {
+                    if (f == e) continue;
+                    const int x = (pe - 1) + 3 * (L.pe[f] - 1);
+                    const R X = L.S[e] * L.v1[f] - L.S[f] * L.v1[e];
+                    const R Y = L.v1[e] - L.v1[f];
+                    const R Z = sqrt(L.v1[e] * L.v1[f]);
+                    const R Q = L.c[pe - 1] - P.E[x];
+                    const R le = ld[e];
+                    lS[e] += le * P.A[x] * L.v1[f];
+                    lS[f] -= le * P.A[x] * L.v1[e];
+                    R dZe = 0, dZf = 0;
+                    if (Z > (R)0) {
+                        dZe = L.v1[f] / ((R)2 * Z);
+                        dZf = L.v1[e] / ((R)2 * Z);
+                    }
+                    lv1[e] += le * (-P.A[x] * L.S[f] + P.B[x] + P.G[x] * Q * dZe);
+                    lv1[f] += le * (P.A[x] * L.S[e] - P.B[x] + P.G[x] * Q * dZf);
+                    lc[pe - 1] += le * P.G[x] * Z;
+                    const R T = P.A[x] * X + P.B[x] * Y + P.G[x] * Z * Q;
+                    gm += (double)le * (double)T / (double)P.s_m;
+                    gs += (double)le * (double)(P.A[x] * X + P.B[x] * Y) / (double)P.s_s;
+                }
+            }
+            // Carbon partition of the driving force: c_p(C, ph_old).
+            R lpo[3] = {0, 0, 0};
+            R addC = 0;
+            for (int p = 0; p < 3; p++) {
+                addC += lc[p] / L.t1[p];
+                for (int j = 0; j < 3; j++) lpo[j] += lc[p] * (-(P.c[p + 3 * j] + L.c[p] * P.k[p + 3 * j]) / L.t1[p]);
+            }
+            lC[n] += addC;
+            // Own slots: v1 (entries from own slots) and ph_old (all own slots).
+            R lo[4] = {0, 0, 0, 0};
+            for (int e = 0; e < L.num; e++)
+                if (L.own[e] >= 0) lo[L.own[e]] += lv1[e];
+            for (int a = 0; a < 4; a++) {
+                const int p = lphase(L.oid[a], P.b1, P.b2);
+                if (p > 0) lo[a] += lpo[p - 1];
+                lphi_pre[4 * n + a] = lo[a];
+            }
+            for (int e = 0; e < L.num; e++) {
+                pub_id[LMAX * n + e] = L.id[e];
+                pub_l[LMAX * n + e] = lS[e];
+            }
+        }
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        gm += __shfl_down_sync(0xffffffffu, gm, s);
+        gs += __shfl_down_sync(0xffffffffu, gs, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (gm != 0) atomicAdd(grad + 0, gm);
+        if (gs != 0) atomicAdd(grad + 1, gs);
+    }
+}
+
+// Reverse of the phase sweep, neighbour part: every slot of cell m that its
+// neighbours scanned (up to the first empty slot) receives the neighbours'
+// published adjoint of their stencil sum for that grain.
+template <typename R>
+__global__ void k_bwd_phase_gather(const AP<R> P, const ushort4 *gid, const int *pub_id, const R *pub_l, R *lphi_pre) {
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= P.N) return;
+    long long nb[6];
+    neighbours(m, P.ix, P.iy, P.iz, nb);
+    const ushort4 g = gid[m];
+    const int id[4] = {g.x, g.y, g.z, g.w};
+    R add[4] = {0, 0, 0, 0};
+    for (int b = 0; b < P.nnb; b++) {
+        const long long n = nb[b];
+        for (int a = 0; a < 4; a++) {
+            if (id[a] == 0) break;
+            for (int e = 0; e < LMAX; e++) {
+                const int t = pub_id[LMAX * n + e];
+                if (t == 0) break;
+                if (t == id[a]) { add[a] += pub_l[LMAX * n + e]; break; }
+            }
+        }
+    }
+    for (int a = 0; a < 4; a++) lphi_pre[4 * m + a] += add[a];
+}
+
+// Reference layout -> calibration layout (carbon only; at most 4 slots kept).
+template <typename R>
+__global__ void k_adj_pack(long long N, pf_f32_map map, const int *ids64, const double *phi64, const double *phase64,
+                           const double *C64, ushort4 *gid, R *phi, R *ph, R *C) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    int l[4];
+    for (int a = 0; a < 4; a++) {
+        const int id = ids64[6 * n + a];
+        int v = 0;
+        if (id > 0) {
+            const int c = id / PF_MAXGRAIN_PER_PHASE;
+            v = map.off[c] + (id - c * PF_MAXGRAIN_PER_PHASE) + (c > 0 ? 1 : 0);
+        }
+        l[a] = v;
+        phi[4 * n + a] = (R)phi64[6 * n + a];
+    }
+    gid[n] = make_ushort4((unsigned short)l[0], (unsigned short)l[1], (unsigned short)l[2], (unsigned short)l[3]);
+    for (int p = 0; p < 3; p++) ph[3 * n + p] = (R)phase64[3 * n + p];
+    C[n] = (R)C64[n];
+}
+
+inline unsigned blocks(long long N) { return (unsigned)((N + 255) / 256); }
+
+}  // namespace
+
+// ============================================================== host side ==
+struct pf_adj_impl {
+    virtual ~pf_adj_impl() {}
+};
+
+template <typename R>
+struct AdjCtx : pf_adj_impl {
+    pf_model model;
+    long long N = 0;
+    int K = 100;
+    cudaStream_t s = nullptr;
+    double scales[4] = {1, 1, 1, 1};
+    double t0 = 0;
+    int nsteps = 0, n_sub = 1;
+    AP<R> P{};
+    // state buffers
+    ushort4 *gid0 = nullptr;
+    R *phi0 = nullptr, *ph0 = nullptr, *C0 = nullptr;        // uploaded initial state
+    std::vector<ushort4 *> ck_gid;                            // checkpoints
+    std::vector<R *> ck_phi, ck_ph, ck_C;
+    // segment storage: per step pre-step state and pre-sub-step carbon
+    std::vector<ushort4 *> sg_gid;
+    std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;
+    ushort4 *w_gid = nullptr;
+    R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
+    // adjoint buffers
+    R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
+    int *pub_id = nullptr;
+    R *pub_l = nullptr;
+    double *d_acc = nullptr;  // 3 objective sums + 4 gradient components
+    double J[2] = {0, 0}, W = 0;
+    double ms_fwd = 0, ms_bwd = 0;
+    pf_f32_map map{};
+    bool have_state = false, have_fwd = false;
+
+    ~AdjCtx() override {
+        cudaStreamSynchronize(s);
+        auto f = [](void *p) { if (p) cudaFree(p); };
+        f(gid0); f(phi0); f(ph0); f(C0);
+        for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
+        for (size_t i = 0; i < sg_gid.size(); i++) { f(sg_gid[i]); f(sg_phi[i]); f(sg_ph[i]); f(sg_C[i]); f(sg_Csub[i]); }
+        f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2);
+        f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
+        if (s) cudaStreamDestroy(s);
+    }
+
+    template <class T>
+    bool alloc(T **p, size_t count) { return cudaMalloc((void **)p, count * sizeof(T)) == cudaSuccess; }
+
+    void params() {
+        pf_step_params p;
+        pf_compute_params(model, t0, p);  // dt and n_sub of the unscaled model, held fixed
+        std::memset(&P, 0, sizeof(P));
+        P.ix = p.ix; P.iy = p.iy; P.iz = p.iz; P.nnb = p.nnb; P.n_sub = p.n_sub; P.N = p.N;
+        P.b1 = map.off[2]; P.b2 = map.off[3];
+        P.cutoff = (R)p.cutoff;
+        const double sm = scales[0], ss = scales[1], sc = scales[2];
+        for (int i = 1; i <= 3; i++)
+            for (int j = 1; j <= 3; j++) {
+                const int e = (i - 1) + 3 * (j - 1);
+                const bool inter = std::abs(i - j) != 2;
+                const double dm = p.pfm_dt * p.m[e] * sm;
+                P.A[e] = inter ? (R)(dm * p.sigma[e] * ss * p.factor1) : (R)0;
+                P.B[e] = inter ? (R)(dm * p.sigma[e] * ss * p.factor2) : (R)0;
+                P.G[e] = (inter && i != j) ? (R)(dm * p.factor3 * p.entropy[e] / p.dcdT[e]) : (R)0;
+                P.E[e] = (R)p.eq[e];
+                P.k[e] = (R)p.k[0][e];
+                P.c[e] = (R)p.c[0][e];
+            }
+        for (int q = 0; q < 3; q++) P.D[q] = (R)(p.D[0][q] * sc * p.coef_diff);
+        P.s_m = (R)sm; P.s_s = (R)ss; P.s_c = (R)sc;
+        n_sub = p.n_sub;
+    }
+
+    int step(const ushort4 *g, const R *phi, const R *ph, const R *C, ushort4 *g2, R *phi2, R *ph2, R *C2,
+             R *Csub /* n_sub*N or null */) {
+        const unsigned nb = blocks(N);
+        k_fwd_phase<R><<<nb, 256, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2);
+        // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
+        // one lands in C2 and no sub-step reads the buffer it writes.
+        R *buf[2] = {C2, w_C2};
+        const R *cin = C;
+        for (int k = 0; k < n_sub; k++) {
+            if (Csub) cudaMemcpyAsync(Csub + (size_t)k * N, cin, N * sizeof(R), cudaMemcpyDeviceToDevice, s);
+            R *cout = buf[(n_sub - 1 - k) % 2];
+            k_fwd_diffuse<R><<<nb, 256, 0, s>>>(P, ph2, cin, cout);
+            cin = cout;
+        }
+        return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
+    }
+};
+
+struct pf_adj {
+    int prec;
+    pf_adj_impl *impl;
+};
+
+template <typename R>
+static AdjCtx<R> *as(pf_adj *a) { return static_cast<AdjCtx<R> *>(a->impl); }
+
+template <typename R>
+static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
+    auto *c = new AdjCtx<R>();
+    c->model = *m;
+    c->N = (long long)m->ix * m->iy * m->iz;
+    c->K = K;
+    const size_t N = (size_t)c->N;
+    bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
+    ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
+         c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
+    ok = ok && c->alloc(&c->l_phi, 4 * N) && c->alloc(&c->l_ph, 3 * N) && c->alloc(&c->l_C, N) &&
+         c->alloc(&c->l_phi2, 4 * N) && c->alloc(&c->l_ph2, 3 * N) && c->alloc(&c->l_C2, N);
+    ok = ok && c->alloc(&c->pub_id, LMAX * N) && c->alloc(&c->pub_l, LMAX * N) && c->alloc(&c->d_acc, 8);
+    if (!ok) {
+        cudaGetLastError();
+        delete c;
+        return pf_fail(PF_ERR_NOMEM, "pf_adj_create: allocation failed");
+    }
+    *out = c;
+    return PF_OK;
+}
+
+extern "C" int pf_adj_create(const pf_model *model, int precision, int checkpoint_every, pf_adj **out) {
+    if (!model || !out || checkpoint_every < 1) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad arguments");
+    if (precision != PF_PREC_FP64 && precision != PF_PREC_FP32C) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad precision");
+    *out = nullptr;
+    pf_adj *a = new pf_adj();
+    a->prec = precision;
+    int st = precision == PF_PREC_FP64 ? adj_create<double>(model, checkpoint_every, &a->impl)
+                                       : adj_create<float>(model, checkpoint_every, &a->impl);
+    if (st != PF_OK) {
+        delete a;
+        return st;
+    }
+    *out = a;
+    return PF_OK;
+}
+
+extern "C" int pf_adj_destroy(pf_adj *a) {
+    if (!a) return PF_OK;
+    delete a->impl;
+    delete a;
+    return PF_OK;
+}
+
+template <typename R>
+static int adj_upload(AdjCtx<R> *c, const int32_t *ids, const double *phi, const double *phase, const double *C,
+                      double time) {
+    const size_t N = (size_t)c->N;
+    int *d_ids = nullptr;
+    double *d_phi = nullptr, *d_phase = nullptr, *d_C = nullptr;
+    int *d_span = nullptr;
+    bool ok = cudaMalloc(&d_ids, 6 * N * sizeof(int)) == cudaSuccess && cudaMalloc(&d_phi, 6 * N * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&d_phase, 3 * N * sizeof(double)) == cudaSuccess && cudaMalloc(&d_C, N * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&d_span, 8 * sizeof(int)) == cudaSuccess;
+    int st = PF_OK;
+    if (!ok) {
+        cudaGetLastError();
+        st = pf_fail(PF_ERR_NOMEM, "pf_adj_upload: staging allocation failed");
+    } else {
+        cudaMemcpyAsync(d_ids, ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->s);
+        cudaMemcpyAsync(d_phi, phi, 6 * N * sizeof(double), cudaMemcpyHostToDevice, c->s);
+        cudaMemcpyAsync(d_phase, phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->s);
+        cudaMemcpyAsync(d_C, C, N * sizeof(double), cudaMemcpyHostToDevice, c->s);
+        cudaMemsetAsync(d_span, 0, 8 * sizeof(int), c->s);
+        pf_launch_id_span(d_ids, c->N, d_span, c->s);
+        int span[8];
+        cudaMemcpyAsync(span, d_span, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->s);
+        cudaError_t e = cudaStreamSynchronize(c->s);
+        if (e != cudaSuccess) st = pf_fail(PF_ERR_CUDA, cudaGetErrorString(e));
+        else if (span[4]) st = pf_fail(PF_ERR_RANGE, "pf_adj_upload: grain id outside 0..399999");
+        else {
+            c->map.off[0] = 0; c->map.off[1] = span[0]; c->map.off[2] = span[0] + span[1];
+            c->map.off[3] = span[0] + span[1] + span[2]; c->map.total = c->map.off[3] + span[3];
+            if (c->map.total > 65535) st = pf_fail(PF_ERR_RANGE, "pf_adj_upload: more than 65535 grains");
+        }
+        if (st == PF_OK) {
+            k_adj_pack<R><<<blocks(c->N), 256, 0, c->s>>>(c->N, c->map, d_ids, d_phi, d_phase, d_C, c->gid0, c->phi0,
+                                                        c->ph0, c->C0);
+            if (cudaStreamSynchronize(c->s) != cudaSuccess) st = pf_fail(PF_ERR_CUDA, "pf_adj_upload: pack failed");
+        }
+    }
+    cudaFree(d_ids); cudaFree(d_phi); cudaFree(d_phase); cudaFree(d_C); cudaFree(d_span);
+    if (st == PF_OK) {
+        c->t0 = time;
+        c->have_state = true;
+        c->have_fwd = false;
+    }
+    return st;
+}
+
+extern "C" int pf_adj_upload(pf_adj *a, const int32_t *ids, const double *phi, const double *phase, const double *C,
+                             double time) {
+    if (!a || !ids || !phi || !phase || !C) return pf_fail(PF_ERR_ARG, "pf_adj_upload: null argument");
+    return a->prec == PF_PREC_FP64 ? adj_upload(as<double>(a), ids, phi, phase, C, time)
+                                   : adj_upload(as<float>(a), ids, phi, phase, C, time);
+}
+
+extern "C" int pf_adj_set_scales(pf_adj *a, const double scales[4]) {
+    if (!a || !scales) return pf_fail(PF_ERR_ARG, "pf_adj_set_scales: null argument");
+    double *dst = a->prec == PF_PREC_FP64 ? as<double>(a)->scales : as<float>(a)->scales;
+    for (int i = 0; i < 4; i++) dst[i] = scales[i];
+    if (a->prec == PF_PREC_FP64) as<double>(a)->have_fwd = false;
+    else as<float>(a)->have_fwd = false;
+    return PF_OK;
+}
+
+template <typename R>
+static int ensure_ck(AdjCtx<R> *c, size_t nck, size_t nseg) {
+    const size_t N = (size_t)c->N;
+    while (c->ck_gid.size() < nck) {
+        ushort4 *g; R *p, *h, *C;
+        if (!c->alloc(&g, N) || !c->alloc(&p, 4 * N) || !c->alloc(&h, 3 * N) || !c->alloc(&C, N)) {
+            cudaGetLastError();
+            return pf_fail(PF_ERR_NOMEM, "adjoint checkpoint allocation failed");
+        }
+        c->ck_gid.push_back(g); c->ck_phi.push_back(p); c->ck_ph.push_back(h); c->ck_C.push_back(C);
+    }
+    while (c->sg_gid.size() < nseg) {
+        ushort4 *g; R *p, *h, *C, *Cs;
+        if (!c->alloc(&g, N) || !c->alloc(&p, 4 * N) || !c->alloc(&h, 3 * N) || !c->alloc(&C, N) ||
+            !c->alloc(&Cs, (size_t)c->n_sub * N)) {
+            cudaGetLastError();
+            return pf_fail(PF_ERR_NOMEM, "adjoint segment allocation failed");
+        }
+        c->sg_gid.push_back(g); c->sg_phi.push_back(p); c->sg_ph.push_back(h); c->sg_C.push_back(C); c->sg_Csub.push_back(Cs);
+    }
+    return PF_OK;
+}
+
+template <typename R>
+static void copy_state(AdjCtx<R> *c, const ushort4 *g, const R *p, const R *h, const R *C, ushort4 *g2, R *p2, R *h2,
+                       R *C2) {
+    const size_t N = (size_t)c->N;
+    cudaMemcpyAsync(g2, g, N * sizeof(ushort4), cudaMemcpyDeviceToDevice, c->s);
+    cudaMemcpyAsync(p2, p, 4 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+    cudaMemcpyAsync(h2, h, 3 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+    cudaMemcpyAsync(C2, C, N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+}
+
+template <typename R>
+static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
+    if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_adj_forward: no state uploaded");
+    c->params();
+    c->nsteps = nsteps;
+    const int nck = (nsteps + c->K - 1) / c->K + 1;
+    int st = ensure_ck(c, (size_t)nck, 0);
+    if (st != PF_OK) return st;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->s);
+    // Two state sets alternate: the work buffers and the spare checkpoint slot
+    // (slot nck-1 is never a checkpoint).  Checkpoints are copies taken every K steps.
+    ushort4 *ga = c->w_gid, *gb = c->ck_gid[nck - 1];
+    R *pa = c->w_phi, *pb = c->ck_phi[nck - 1], *ha = c->w_ph, *hb = c->ck_ph[nck - 1];
+    R *Ca = c->w_C, *Cb = c->ck_C[nck - 1];
+    copy_state(c, c->gid0, c->phi0, c->ph0, c->C0, ga, pa, ha, Ca);
+    for (int t = 0; t < nsteps; t++) {
+        if (t % c->K == 0)
+            copy_state(c, ga, pa, ha, Ca, c->ck_gid[t / c->K], c->ck_phi[t / c->K], c->ck_ph[t / c->K], c->ck_C[t / c->K]);
+        st = c->step(ga, pa, ha, Ca, gb, pb, hb, Cb, nullptr);
+        if (st != PF_OK) return st;
+        std::swap(ga, gb); std::swap(pa, pb); std::swap(ha, hb); std::swap(Ca, Cb);
+    }
+    cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
+    AP<R> P = c->P;
+    k_objective_sums<R><<<256, 256, 0, c->s>>>(P, ha, Ca, c->d_acc);
+    double h[8];
+    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaEventRecord(e1, c->s);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_forward failed");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    c->ms_fwd = ms;
+    c->J[0] = h[0] / (double)c->N;
+    c->W = h[1];
+    c->J[1] = h[1] > 0 ? h[2] / h[1] : 0.0;
+    J[0] = c->J[0];
+    J[1] = c->J[1];
+    c->have_fwd = true;
+    return PF_OK;
+}
+
+extern "C" int pf_adj_forward(pf_adj *a, int nsteps, double J[2]) {
+    if (!a || !J || nsteps < 1) return pf_fail(PF_ERR_ARG, "pf_adj_forward: bad arguments");
+    return a->prec == PF_PREC_FP64 ? adj_forward(as<double>(a), nsteps, J) : adj_forward(as<float>(a), nsteps, J);
+}
+
+template <typename R>
+static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
+    if (!c->have_fwd) return pf_fail(PF_ERR_ARG, "pf_adj_gradient: run pf_adj_forward first");
+    const int nck = (c->nsteps + c->K - 1) / c->K + 1;
+    int st = ensure_ck(c, (size_t)nck, (size_t)c->K);
+    if (st != PF_OK) return st;
+    const size_t N = (size_t)c->N;
+    const unsigned nb = blocks(c->N);
+    AP<R> P = c->P;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->s);
+    // Final state: recompute the last segment, then seed from its end state.
+    cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
+    bool seeded = false;
+    const int nseg = (c->nsteps + c->K - 1) / c->K;
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int t0 = sg * c->K, t1 = std::min(c->nsteps, t0 + c->K);
+        // Recompute the segment, storing every pre-step state and pre-sub-step carbon.
+        copy_state(c, c->ck_gid[sg], c->ck_phi[sg], c->ck_ph[sg], c->ck_C[sg], c->sg_gid[0], c->sg_phi[0], c->sg_ph[0], c->sg_C[0]);
+        for (int t = t0; t < t1; t++) {
+            const int i = t - t0;
+            ushort4 *g2 = (i + 1 < c->K) ? c->sg_gid[i + 1] : c->w_gid;
+            R *p2 = (i + 1 < c->K) ? c->sg_phi[i + 1] : c->w_phi;
+            R *h2 = (i + 1 < c->K) ? c->sg_ph[i + 1] : c->w_ph;
+            R *C2 = (i + 1 < c->K) ? c->sg_C[i + 1] : c->w_C;
+            if (t == t1 - 1) { g2 = c->w_gid; p2 = c->w_phi; h2 = c->w_ph; C2 = c->w_C; }
+            st = c->step(c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], g2, p2, h2, C2, c->sg_Csub[i]);
+            if (st != PF_OK) return st;
+        }
+        if (!seeded) {
+            k_seed<R><<<nb, 256, 0, c->s>>>(P, obj, c->w_ph, c->w_C, c->W, c->J[1], c->l_ph, c->l_C, c->l_phi);
+            seeded = true;
+        }
+        for (int t = t1 - 1; t >= t0; t--) {
+            const int i = t - t0;
+            // Post-sweep phase fractions of step t: recompute the sweep into work buffers.
+            k_fwd_phase<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->w_gid, c->w_phi,
+                                                c->w_ph);
+            // Reverse the diffusion sub-steps (phase fractions fixed at the post-sweep values).
+            for (int k = c->n_sub - 1; k >= 0; k--) {
+                k_bwd_diffuse<R><<<nb, 256, 0, c->s>>>(P, c->w_ph, c->sg_Csub[i] + (size_t)k * N, c->l_C, c->l_C2, c->l_ph,
+                                                      c->d_acc + 3);
+                std::swap(c->l_C, c->l_C2);
+            }
+            // Reverse the phase sweep.
+            k_bwd_phase_own<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
+                                                    c->l_ph, c->l_C, c->l_phi2, c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
+            k_bwd_phase_gather<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->pub_id, c->pub_l, c->l_phi2);
+            std::swap(c->l_phi, c->l_phi2);
+            std::swap(c->l_ph, c->l_ph2);
+        }
+    }
+    double h[8];
+    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaEventRecord(e1, c->s);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_gradient failed");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    c->ms_bwd = ms;
+    grad[0] = h[3];
+    grad[1] = h[4];
+    grad[2] = h[5];
+    grad[3] = 0.0;  // Mn does not enter the phase update or the carbon field
+    return PF_OK;
+}
+
+extern "C" int pf_adj_gradient(pf_adj *a, int objective, double grad[4]) {
+    if (!a || !grad || objective < 0 || objective > 1) return pf_fail(PF_ERR_ARG, "pf_adj_gradient: bad arguments");
+    return a->prec == PF_PREC_FP64 ? adj_gradient(as<double>(a), objective, grad)
+                                   : adj_gradient(as<float>(a), objective, grad);
+}
+
+extern "C" int pf_adj_timings(pf_adj *a, double ms[2]) {
+    if (!a || !ms) return pf_fail(PF_ERR_ARG, "pf_adj_timings: null argument");
+    if (a->prec == PF_PREC_FP64) { ms[0] = as<double>(a)->ms_fwd; ms[1] = as<double>(a)->ms_bwd; }
+    else { ms[0] = as<float>(a)->ms_fwd; ms[1] = as<float>(a)->ms_bwd; }
+    return PF_OK;
+}
