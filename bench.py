@@ -214,6 +214,44 @@ def run_batch(args, rank: int) -> dict:
             "austenite_fraction_first_domains": fr}
 
 
+def run_adjoint(args) -> dict:
+    """Adjoint calibration: 2D 512^2, ferrite + austenite + cementite particles
+    (radius 2, 0.5% area), FP32 with FP64 reductions, checkpoint every 100
+    steps.  Ratio = (gradient time, recomputation included) / (forward time)."""
+    import phasefield_gb300 as pf
+    from phasefield_gb300 import workloads as W
+
+    wl = W.WORKLOADS["2d512cem"]
+    cfg, m = _model_for(wl)
+    st = pf.init_microstructure(m, wl.spec(), 0.0)
+    A = pf.Adjoint(m, pf.PF_PREC_FP32C, 100)
+    A.upload(st, 0.0)
+    A.forward(min(args.adjoint_steps, 100))  # warm-up
+    J = A.forward(args.adjoint_steps)
+    g = A.gradient(0)
+    t = A.timings()
+    A.close()
+    # The production FP32C forward on the same state, for scale.
+    import torch
+
+    F = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    F.upload(st, 0.0)
+    F.update(10)
+    F.synchronize()
+    t0 = time.perf_counter()
+    F.update(args.adjoint_steps)
+    F.synchronize()
+    prod_ms = (time.perf_counter() - t0) * 1e3
+    F.close()
+    torch.cuda.synchronize()
+    return {"grid": list(wl.grid), "steps": args.adjoint_steps, "checkpoint_every": 100,
+            "production_forward_ms": prod_ms, "adjoint_over_production_forward": t["gradient_ms"] / prod_ms,
+            "J_ferrite_fraction": float(J[0]), "J_austenite_carbon": float(J[1]),
+            "dJ0_ds": [float(x) for x in g], "forward_ms": t["forward_ms"], "gradient_ms": t["gradient_ms"],
+            "adjoint_over_forward": t["gradient_ms"] / t["forward_ms"],
+            "note": "gradient_ms covers segment recomputation from checkpoints and the reverse sweep"}
+
+
 def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     import numpy as np
     import torch
@@ -420,6 +458,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the diffusion tile autotuner")
     ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-domain ensemble (0 = skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint calibration run (0 = skip)")
     ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -448,6 +487,8 @@ def main() -> None:
         b = run_batch(args, rank)
         if out is not None:
             out["batch"] = b
+    if args.adjoint_steps > 0 and out is not None:
+        out["adjoint"] = run_adjoint(args)
     if out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:

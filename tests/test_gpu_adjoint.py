@@ -62,6 +62,20 @@ def test_gradient_independent_of_checkpoint_interval(gpu, tmp_path):
         np.testing.assert_allclose(g, out[0], rtol=1e-10, atol=1e-300)
 
 
+def test_torch_autograd_wrapper(gpu, tmp_path):
+    import torch
+
+    from phasefield_gb300 import calibration
+
+    A = _setup(tmp_path)
+    s = torch.ones(4, dtype=torch.float64, requires_grad=True)
+    J = calibration.objective(s, A, 10, 1)
+    J.backward()
+    g = A.gradient(1)
+    np.testing.assert_allclose(s.grad.numpy(), g, rtol=1e-12)
+    assert J.item() == pytest.approx(A.forward(10)[1], rel=1e-12)
+
+
 def test_fp32_gradient_tracks_fp64(gpu, tmp_path):
     steps = 12
     g64 = _setup(tmp_path, pf.PF_PREC_FP64)
