@@ -188,35 +188,82 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
     for (int p = 0; p < 3; p++) ph2[3 * n + p] = q[p] * inv;
 }
 
-// Flux of one cell (the forward sub-step's increment), neighbours partitioned on the fly.
+// Per-cell derived quantities of one sub-step, formed once: s_p = sqrt(phi_p),
+// c_p (partitioned carbon) and 1/t1_p, each as three planes.
 template <typename R>
-__device__ R flux_at(const AP<R> &P, long long n, const R *ph, const R *C) {
-    long long nb[6];
-    neighbours(n, P.ix, P.iy, P.iz, nb);
-    const R p0[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
-    R c0[3], t0[3];
-    partition(P, C[n], p0, c0, t0);
-    R f = 0;
-    for (int p = 0; p < 3; p++) {
-        const R s0 = sqrt(p0[p]);
-        R a = 0;
-        for (int b = 0; b < P.nnb; b++) {
-            const long long m = nb[b];
-            const R pm[3] = {ph[3 * m], ph[3 * m + 1], ph[3 * m + 2]};
-            R cm[3], tm[3];
-            partition(P, C[m], pm, cm, tm);
-            a += sqrt(pm[p]) * (cm[p] - c0[p]);
-        }
-        f += s0 * P.D[p] * a;
-    }
-    return f;
-}
-
-template <typename R>
-__global__ void k_fwd_diffuse(const AP<R> P, const R *ph, const R *C, R *C2) {
+__global__ void k_derive(const AP<R> P, const R *ph, const R *C, R *ds, R *dc, R *dit) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= P.N) return;
-    C2[n] = C[n] + flux_at(P, n, ph, C);
+    const R p[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+    R c[3], t[3];
+    partition(P, C[n], p, c, t);
+    for (int q = 0; q < 3; q++) {
+        ds[q * P.N + n] = sqrt(p[q]);
+        dc[q * P.N + n] = c[q];
+        dit[q * P.N + n] = (R)1 / t[q];
+    }
+}
+
+// Forward sub-step (solver.cpp:343-372) from the derived planes:
+//   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p).
+template <typename R>
+__global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.N) return;
+    long long nb[6];
+    neighbours(n, P.ix, P.iy, P.iz, nb);
+    R f = 0;
+    for (int p = 0; p < 3; p++) {
+        const R c0 = dc[p * P.N + n];
+        R a = 0;
+        for (int b = 0; b < P.nnb; b++) a += ds[p * P.N + nb[b]] * (dc[p * P.N + nb[b]] - c0);
+        f += ds[p * P.N + n] * P.D[p] * a;
+    }
+    C2[n] = C[n] + f;
+}
+
+// Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
+// sub-step), the derived planes of the state before it, ph.  Out: lam2
+// (adjoint of C before), lph += the phase-fraction part (through s_p and
+// c_p(phi)), grad[2] += dJ/ds_C.
+template <typename R>
+__global__ void k_bwd_diffuse_d(const AP<R> P, const R *ph, const R *ds, const R *dc, const R *dit, const R *lam,
+                                R *lam2, R *lph, double *grad) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double g = 0;
+    if (n < P.N) {
+        long long nb[6];
+        neighbours(n, P.ix, P.iy, P.iz, nb);
+        const R l0 = lam[n];
+        R out = l0, dL_ds[3], dL_dc[3], flux = 0;
+        for (int p = 0; p < 3; p++) {
+            const R s0 = ds[p * P.N + n], c0 = dc[p * P.N + n];
+            R al = 0, ac = 0, ads = 0;
+            for (int b = 0; b < P.nnb; b++) {
+                const long long m = nb[b];
+                const R sm = ds[p * P.N + m], dcm = dc[p * P.N + m] - c0, lm = lam[m];
+                al += sm * (lm - l0);
+                ac += sm * dcm;
+                ads += sm * dcm * (l0 - lm);
+            }
+            out += P.D[p] * s0 * dit[p * P.N + n] * al;
+            dL_dc[p] = P.D[p] * s0 * al;
+            dL_ds[p] = P.D[p] * ads;
+            flux += s0 * P.D[p] * ac;
+        }
+        lam2[n] = out;
+        for (int j = 0; j < 3; j++) {
+            R v = 0;
+            for (int p = 0; p < 3; p++)
+                v += dL_dc[p] * (-(P.c[p + 3 * j] + dc[p * P.N + n] * P.k[p + 3 * j]) * dit[p * P.N + n]);
+            const R sj = ds[j * P.N + n];
+            if (sj > (R)0) v += dL_ds[j] / ((R)2 * sj);
+            lph[3 * n + j] += v;
+        }
+        g = (double)l0 * (double)flux / (double)P.s_c;
+    }
+    for (int s = 16; s > 0; s >>= 1) g += __shfl_down_sync(0xffffffffu, g, s);
+    if ((threadIdx.x & 31) == 0 && g != 0) atomicAdd(grad + 2, g);
 }
 
 // Objective sums in FP64: out[0] = sum phi_1, out[1] = sum phi_2, out[2] = sum phi_2 c_2.
@@ -268,54 +315,6 @@ __global__ void k_seed(const AP<R> P, int obj, const R *ph, const R *C, double W
         if (j == 1) v += c[1] - (R)J;
         lph[3 * n + j] = v * iw;
     }
-}
-
-// Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
-// sub-step), C (before it), ph.  Out: lam2 (adjoint of C before), lph += the
-// phase-fraction part, grad[2] += dJ/ds_C.
-template <typename R>
-__global__ void k_bwd_diffuse(const AP<R> P, const R *ph, const R *C, const R *lam, R *lam2, R *lph, double *grad) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double g = 0;
-    if (n < P.N) {
-        long long nb[6];
-        neighbours(n, P.ix, P.iy, P.iz, nb);
-        const R p0[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
-        R c0[3], t0[3];
-        partition(P, C[n], p0, c0, t0);
-        const R l0 = lam[n];
-        R out = l0;
-        R dL_ds[3] = {0, 0, 0}, dL_dc[3] = {0, 0, 0};
-        R flux = 0;
-        for (int p = 0; p < 3; p++) {
-            const R s0 = sqrt(p0[p]);
-            R al = 0, ac = 0, ads = 0;
-            for (int b = 0; b < P.nnb; b++) {
-                const long long m = nb[b];
-                const R pm[3] = {ph[3 * m], ph[3 * m + 1], ph[3 * m + 2]};
-                R cm[3], tm[3];
-                partition(P, C[m], pm, cm, tm);
-                const R sm = sqrt(pm[p]);
-                al += sm * (lam[m] - l0);
-                ac += sm * (cm[p] - c0[p]);
-                ads += sm * (cm[p] - c0[p]) * (l0 - lam[m]);
-            }
-            out += P.D[p] * s0 / t0[p] * al;
-            dL_dc[p] = P.D[p] * s0 * al;
-            dL_ds[p] = P.D[p] * ads;
-            flux += s0 * P.D[p] * ac;
-        }
-        lam2[n] = out;
-        for (int j = 0; j < 3; j++) {
-            R v = 0;
-            for (int p = 0; p < 3; p++) v += dL_dc[p] * (-(P.c[p + 3 * j] + c0[p] * P.k[p + 3 * j]) / t0[p]);
-            if (p0[j] > 0) v += dL_ds[j] / ((R)2 * sqrt(p0[j]));
-            lph[3 * n + j] += v;
-        }
-        g = (double)l0 * (double)flux / (double)P.s_c;
-    }
-    for (int s = 16; s > 0; s >>= 1) g += __shfl_down_sync(0xffffffffu, g, s);
-    if ((threadIdx.x & 31) == 0 && g != 0) atomicAdd(grad + 2, g);
 }
 
 // Reverse of the phase sweep, own-cell part.  In: pre-step state, lam_phi /
@@ -500,6 +499,7 @@ struct AdjCtx : pf_adj_impl {
     std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;
     ushort4 *w_gid = nullptr;
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
+    R *d_s = nullptr, *d_c = nullptr, *d_it = nullptr;  // derived planes of one sub-step
     // adjoint buffers
     R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
     int *pub_id = nullptr;
@@ -516,7 +516,7 @@ struct AdjCtx : pf_adj_impl {
         f(gid0); f(phi0); f(ph0); f(C0);
         for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
         for (size_t i = 0; i < sg_gid.size(); i++) { f(sg_gid[i]); f(sg_phi[i]); f(sg_ph[i]); f(sg_C[i]); f(sg_Csub[i]); }
-        f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2);
+        f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(d_s); f(d_c); f(d_it);
         f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
         if (s) cudaStreamDestroy(s);
     }
@@ -560,7 +560,8 @@ struct AdjCtx : pf_adj_impl {
         for (int k = 0; k < n_sub; k++) {
             if (Csub) cudaMemcpyAsync(Csub + (size_t)k * N, cin, N * sizeof(R), cudaMemcpyDeviceToDevice, s);
             R *cout = buf[(n_sub - 1 - k) % 2];
-            k_fwd_diffuse<R><<<nb, 256, 0, s>>>(P, ph2, cin, cout);
+            k_derive<R><<<nb, 256, 0, s>>>(P, ph2, cin, d_s, d_c, d_it);
+            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, d_s, d_c, cin, cout);
             cin = cout;
         }
         return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
@@ -584,6 +585,7 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     const size_t N = (size_t)c->N;
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
+    ok = ok && c->alloc(&c->d_s, 3 * N) && c->alloc(&c->d_c, 3 * N) && c->alloc(&c->d_it, 3 * N);
     ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
          c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
     ok = ok && c->alloc(&c->l_phi, 4 * N) && c->alloc(&c->l_ph, 3 * N) && c->alloc(&c->l_C, N) &&
@@ -801,13 +803,15 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
         }
         for (int t = t1 - 1; t >= t0; t--) {
             const int i = t - t0;
-            // Post-sweep phase fractions of step t: recompute the sweep into work buffers.
-            k_fwd_phase<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->w_gid, c->w_phi,
-                                                c->w_ph);
-            // Reverse the diffusion sub-steps (phase fractions fixed at the post-sweep values).
+            // Post-sweep phase fractions of step t: the diffusion leaves them
+            // alone, so they are the next step's stored pre-step values (or the
+            // segment's end state for its last step).
+            const R *ph_post = (t + 1 < t1) ? c->sg_ph[i + 1] : c->w_ph;
+            // Reverse the diffusion sub-steps.
             for (int k = c->n_sub - 1; k >= 0; k--) {
-                k_bwd_diffuse<R><<<nb, 256, 0, c->s>>>(P, c->w_ph, c->sg_Csub[i] + (size_t)k * N, c->l_C, c->l_C2, c->l_ph,
-                                                      c->d_acc + 3);
+                k_derive<R><<<nb, 256, 0, c->s>>>(P, ph_post, c->sg_Csub[i] + (size_t)k * N, c->d_s, c->d_c, c->d_it);
+                k_bwd_diffuse_d<R><<<nb, 256, 0, c->s>>>(P, ph_post, c->d_s, c->d_c, c->d_it, c->l_C, c->l_C2, c->l_ph,
+                                                        c->d_acc + 3);
                 std::swap(c->l_C, c->l_C2);
             }
             // Reverse the phase sweep.
