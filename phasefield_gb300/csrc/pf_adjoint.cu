@@ -509,9 +509,20 @@ struct AdjCtx : pf_adj_impl {
     double ms_fwd = 0, ms_bwd = 0;
     pf_f32_map map{};
     bool have_state = false, have_fwd = false;
+    // Graphs of one full checkpoint segment: forward (per starting buffer set)
+    // and recompute + reverse sweep.  Rebuilt whenever the parameters change.
+    cudaGraphExec_t fwd_graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t seg_graph = nullptr;
+
+    void drop_graphs() {
+        for (auto &g : fwd_graph)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        if (seg_graph) { cudaGraphExecDestroy(seg_graph); seg_graph = nullptr; }
+    }
 
     ~AdjCtx() override {
         cudaStreamSynchronize(s);
+        drop_graphs();
         auto f = [](void *p) { if (p) cudaFree(p); };
         f(gid0); f(phi0); f(ph0); f(C0);
         for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
@@ -735,12 +746,43 @@ static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
     R *pa = c->w_phi, *pb = c->ck_phi[nck - 1], *ha = c->w_ph, *hb = c->ck_ph[nck - 1];
     R *Ca = c->w_C, *Cb = c->ck_C[nck - 1];
     copy_state(c, c->gid0, c->phi0, c->ph0, c->C0, ga, pa, ha, Ca);
-    for (int t = 0; t < nsteps; t++) {
-        if (t % c->K == 0)
-            copy_state(c, ga, pa, ha, Ca, c->ck_gid[t / c->K], c->ck_phi[t / c->K], c->ck_ph[t / c->K], c->ck_C[t / c->K]);
-        st = c->step(ga, pa, ha, Ca, gb, pb, hb, Cb, nullptr);
+    c->drop_graphs();
+    // A full segment of K steps is one CUDA graph (per starting buffer set);
+    // the checkpoint copy in front of it depends on the segment and stays outside.
+    auto run_steps = [&](int n) -> int {
+        for (int t = 0; t < n; t++) {
+            int s2 = c->step(ga, pa, ha, Ca, gb, pb, hb, Cb, nullptr);
+            if (s2 != PF_OK) return s2;
+            std::swap(ga, gb); std::swap(pa, pb); std::swap(ha, hb); std::swap(Ca, Cb);
+        }
+        return PF_OK;
+    };
+    for (int t = 0; t < nsteps; t += c->K) {
+        const int n = std::min(c->K, nsteps - t);
+        copy_state(c, ga, pa, ha, Ca, c->ck_gid[t / c->K], c->ck_phi[t / c->K], c->ck_ph[t / c->K], c->ck_C[t / c->K]);
+        if (n < c->K) {
+            st = run_steps(n);
+        } else {
+            const int set = (ga == c->w_gid) ? 0 : 1;
+            if (!c->fwd_graph[set]) {
+                cudaGraph_t g;
+                if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                    return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+                st = run_steps(n);
+                if (cudaStreamEndCapture(c->s, &g) != cudaSuccess || st != PF_OK)
+                    return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+                const bool okg = cudaGraphInstantiate(&c->fwd_graph[set], g, 0) == cudaSuccess;
+                cudaGraphDestroy(g);
+                if (!okg) return pf_fail(PF_ERR_CUDA, "adjoint: graph instantiation failed");
+            } else {
+                // Replay: the host-side buffer roles advance as during capture.
+                for (int q = 0; q < n; q++) {
+                    std::swap(ga, gb); std::swap(pa, pb); std::swap(ha, hb); std::swap(Ca, Cb);
+                }
+            }
+            if (cudaGraphLaunch(c->fwd_graph[set], c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
+        }
         if (st != PF_OK) return st;
-        std::swap(ga, gb); std::swap(pa, pb); std::swap(ha, hb); std::swap(Ca, Cb);
     }
     cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
     AP<R> P = c->P;
@@ -783,10 +825,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
     bool seeded = false;
     const int nseg = (c->nsteps + c->K - 1) / c->K;
-    for (int sg = nseg - 1; sg >= 0; sg--) {
-        const int t0 = sg * c->K, t1 = std::min(c->nsteps, t0 + c->K);
-        // Recompute the segment, storing every pre-step state and pre-sub-step carbon.
-        copy_state(c, c->ck_gid[sg], c->ck_phi[sg], c->ck_ph[sg], c->ck_C[sg], c->sg_gid[0], c->sg_phi[0], c->sg_ph[0], c->sg_C[0]);
+    auto recompute = [&](int t0, int t1) -> int {
         for (int t = t0; t < t1; t++) {
             const int i = t - t0;
             ushort4 *g2 = (i + 1 < c->K) ? c->sg_gid[i + 1] : c->w_gid;
@@ -794,13 +833,12 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
             R *h2 = (i + 1 < c->K) ? c->sg_ph[i + 1] : c->w_ph;
             R *C2 = (i + 1 < c->K) ? c->sg_C[i + 1] : c->w_C;
             if (t == t1 - 1) { g2 = c->w_gid; p2 = c->w_phi; h2 = c->w_ph; C2 = c->w_C; }
-            st = c->step(c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], g2, p2, h2, C2, c->sg_Csub[i]);
-            if (st != PF_OK) return st;
+            int s2 = c->step(c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], g2, p2, h2, C2, c->sg_Csub[i]);
+            if (s2 != PF_OK) return s2;
         }
-        if (!seeded) {
-            k_seed<R><<<nb, 256, 0, c->s>>>(P, obj, c->w_ph, c->w_C, c->W, c->J[1], c->l_ph, c->l_C, c->l_phi);
-            seeded = true;
-        }
+        return PF_OK;
+    };
+    auto reverse = [&](int t0, int t1) {
         for (int t = t1 - 1; t >= t0; t--) {
             const int i = t - t0;
             // Post-sweep phase fractions of step t: the diffusion leaves them
@@ -821,6 +859,51 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
             std::swap(c->l_phi, c->l_phi2);
             std::swap(c->l_ph, c->l_ph2);
         }
+    };
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int t0 = sg * c->K, t1 = std::min(c->nsteps, t0 + c->K);
+        // Recompute the segment from its checkpoint, storing every pre-step
+        // state and pre-sub-step carbon, then sweep it backwards.
+        copy_state(c, c->ck_gid[sg], c->ck_phi[sg], c->ck_ph[sg], c->ck_C[sg], c->sg_gid[0], c->sg_phi[0], c->sg_ph[0],
+                   c->sg_C[0]);
+        if (!seeded || t1 - t0 != c->K) {
+            st = recompute(t0, t1);
+            if (st != PF_OK) return st;
+            if (!seeded) {
+                k_seed<R><<<nb, 256, 0, c->s>>>(P, obj, c->w_ph, c->w_C, c->W, c->J[1], c->l_ph, c->l_C, c->l_phi);
+                seeded = true;
+            }
+            reverse(t0, t1);
+            continue;
+        }
+        // Every other segment is identical launch for launch: one graph,
+        // captured once, ending with the adjoint buffers back in their roles.
+        if (!c->seg_graph) {
+            R *cC = c->l_C, *cphi = c->l_phi, *cph = c->l_ph;
+            cudaGraph_t g;
+            if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+            st = recompute(t0, t1);
+            reverse(t0, t1);
+            if (c->l_C != cC) {
+                cudaMemcpyAsync(cC, c->l_C, N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_C, c->l_C2);
+            }
+            if (c->l_phi != cphi) {
+                cudaMemcpyAsync(cphi, c->l_phi, 4 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_phi, c->l_phi2);
+            }
+            if (c->l_ph != cph) {
+                cudaMemcpyAsync(cph, c->l_ph, 3 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_ph, c->l_ph2);
+            }
+            if (cudaStreamEndCapture(c->s, &g) != cudaSuccess || st != PF_OK)
+                return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+            const bool okg = cudaGraphInstantiate(&c->seg_graph, g, 0) == cudaSuccess;
+            cudaGraphDestroy(g);
+            if (!okg) return pf_fail(PF_ERR_CUDA, "adjoint: graph instantiation failed");
+        }
+        if (cudaGraphLaunch(c->seg_graph, c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
     }
     double h[8];
     cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
