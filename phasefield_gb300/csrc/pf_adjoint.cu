@@ -28,7 +28,9 @@
 //   cell; the neighbour sums S_e = sum_nb phi_nb(e) are returned to the
 //   neighbours' slots by a gather over the neighbours' published lists.
 // Checkpoints every K steps; a segment is recomputed forward storing every
-// step's pre-step state and pre-sub-step carbon, then swept backwards.
+// step's pre-step state and every sub-step's derived planes (s_p, c_p, 1/t1_p;
+// HBM is plentiful), then swept backwards.  Full segments are replayed from one
+// captured CUDA graph.
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -513,6 +515,7 @@ struct AdjCtx : pf_adj_impl {
     // and recompute + reverse sweep.  Rebuilt whenever the parameters change.
     cudaGraphExec_t fwd_graph[2] = {nullptr, nullptr};
     cudaGraphExec_t seg_graph = nullptr;
+    R *g_C = nullptr, *g_phi = nullptr, *g_ph = nullptr;  // adjoint buffer roles at capture
 
     void drop_graphs() {
         for (auto &g : fwd_graph)
@@ -560,8 +563,10 @@ struct AdjCtx : pf_adj_impl {
         n_sub = p.n_sub;
     }
 
+    // One forward step.  With Dsub (n_sub * 9N values) the derived planes of
+    // every sub-step (s_p, c_p, 1/t1_p) are kept there for the reverse sweep.
     int step(const ushort4 *g, const R *phi, const R *ph, const R *C, ushort4 *g2, R *phi2, R *ph2, R *C2,
-             R *Csub /* n_sub*N or null */) {
+             R *Dsub) {
         const unsigned nb = blocks(N);
         k_fwd_phase<R><<<nb, 256, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
@@ -569,10 +574,12 @@ struct AdjCtx : pf_adj_impl {
         R *buf[2] = {C2, w_C2};
         const R *cin = C;
         for (int k = 0; k < n_sub; k++) {
-            if (Csub) cudaMemcpyAsync(Csub + (size_t)k * N, cin, N * sizeof(R), cudaMemcpyDeviceToDevice, s);
             R *cout = buf[(n_sub - 1 - k) % 2];
-            k_derive<R><<<nb, 256, 0, s>>>(P, ph2, cin, d_s, d_c, d_it);
-            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, d_s, d_c, cin, cout);
+            R *ds = Dsub ? Dsub + (size_t)k * 9 * N : d_s;
+            R *dc = Dsub ? ds + 3 * N : d_c;
+            R *dit = Dsub ? ds + 6 * N : d_it;
+            k_derive<R><<<nb, 256, 0, s>>>(P, ph2, cin, ds, dc, dit);
+            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, ds, dc, cin, cout);
             cin = cout;
         }
         return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
@@ -710,7 +717,7 @@ static int ensure_ck(AdjCtx<R> *c, size_t nck, size_t nseg) {
     while (c->sg_gid.size() < nseg) {
         ushort4 *g; R *p, *h, *C, *Cs;
         if (!c->alloc(&g, N) || !c->alloc(&p, 4 * N) || !c->alloc(&h, 3 * N) || !c->alloc(&C, N) ||
-            !c->alloc(&Cs, (size_t)c->n_sub * N)) {
+            !c->alloc(&Cs, (size_t)c->n_sub * 9 * N)) {
             cudaGetLastError();
             return pf_fail(PF_ERR_NOMEM, "adjoint segment allocation failed");
         }
@@ -847,8 +854,8 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
             const R *ph_post = (t + 1 < t1) ? c->sg_ph[i + 1] : c->w_ph;
             // Reverse the diffusion sub-steps.
             for (int k = c->n_sub - 1; k >= 0; k--) {
-                k_derive<R><<<nb, 256, 0, c->s>>>(P, ph_post, c->sg_Csub[i] + (size_t)k * N, c->d_s, c->d_c, c->d_it);
-                k_bwd_diffuse_d<R><<<nb, 256, 0, c->s>>>(P, ph_post, c->d_s, c->d_c, c->d_it, c->l_C, c->l_C2, c->l_ph,
+                const R *ds = c->sg_Csub[i] + (size_t)k * 9 * N;
+                k_bwd_diffuse_d<R><<<nb, 256, 0, c->s>>>(P, ph_post, ds, ds + 3 * N, ds + 6 * N, c->l_C, c->l_C2, c->l_ph,
                                                         c->d_acc + 3);
                 std::swap(c->l_C, c->l_C2);
             }
@@ -863,7 +870,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     for (int sg = nseg - 1; sg >= 0; sg--) {
         const int t0 = sg * c->K, t1 = std::min(c->nsteps, t0 + c->K);
         // Recompute the segment from its checkpoint, storing every pre-step
-        // state and pre-sub-step carbon, then sweep it backwards.
+        // state and every sub-step's derived planes, then sweep it backwards.
         copy_state(c, c->ck_gid[sg], c->ck_phi[sg], c->ck_ph[sg], c->ck_C[sg], c->sg_gid[0], c->sg_phi[0], c->sg_ph[0],
                    c->sg_C[0]);
         if (!seeded || t1 - t0 != c->K) {
@@ -878,8 +885,23 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
         }
         // Every other segment is identical launch for launch: one graph,
         // captured once, ending with the adjoint buffers back in their roles.
-        if (!c->seg_graph) {
+        if (c->seg_graph) {
+            // Replays start from the buffer roles of the capture.
+            if (c->l_C != c->g_C) {
+                cudaMemcpyAsync(c->g_C, c->l_C, N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_C, c->l_C2);
+            }
+            if (c->l_phi != c->g_phi) {
+                cudaMemcpyAsync(c->g_phi, c->l_phi, 4 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_phi, c->l_phi2);
+            }
+            if (c->l_ph != c->g_ph) {
+                cudaMemcpyAsync(c->g_ph, c->l_ph, 3 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+                std::swap(c->l_ph, c->l_ph2);
+            }
+        } else {
             R *cC = c->l_C, *cphi = c->l_phi, *cph = c->l_ph;
+            c->g_C = cC; c->g_phi = cphi; c->g_ph = cph;
             cudaGraph_t g;
             if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
                 return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
