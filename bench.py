@@ -199,12 +199,16 @@ def run_batch(args, rank: int) -> dict:
     B = pf.Batch(models)
     for d, (m, dom) in enumerate(zip(models, doms)):
         B.upload(d, pf.init_microstructure(m, W.ensemble_spec(dom), 0.0), 0.0)
+    from phasefield_gb300 import replicas
+
     st = B.run(args.warmup)
     torch.cuda.synchronize()
+    replicas.barrier()
     t0 = time.perf_counter()
     st2 = B.run(args.batch_steps)
-    dt = time.perf_counter() - t0
+    dt = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda" if replicas.world()[1] > 1 else None)
     info = B.info()
+    info["cells"] = sum(replicas.gather([info["cells"]]))  # every rank advances its own ensemble
     fr = [float(B.reduce(d)[1] / (m.ix * m.iy)) for d, m in enumerate(models[:4])]
     B.close()
     return {"domains": len(models), "cells": info["cells"], "steps": args.batch_steps, "resident_blocks": info["blocks"],
