@@ -256,6 +256,55 @@ def run_adjoint(args) -> dict:
             "note": "gradient_ms covers segment recomputation from checkpoints and the reverse sweep"}
 
 
+def run_precision(args) -> dict:
+    """Error of the FP32-compensated path against FP64 on a 128^3 box of the 3D
+    workload (same grain/nucleus densities) after --precision-steps steps:
+    against the four-slot model in FP64 (the calibration model: isolates FP32
+    rounding) and against the six-slot FP64 reference path (adds the model
+    change of keeping four grains per cell)."""
+    import numpy as np
+
+    import phasefield_gb300 as pf
+
+    wl = _workload(args.workload)
+    grid = (128, 128, 128) if wl.grid[2] > 1 else (256, 256, 1)
+    cfg, m = _model_for(wl, grid)
+    st = pf.init_microstructure(m, _scaled_spec(wl, grid), 0.0)
+    N = grid[0] * grid[1] * grid[2]
+    S = args.precision_steps
+    F32 = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    F32.upload(st, 0.0)
+    F32.update(S)
+    a32 = F32.download(conc=False)
+    r32 = F32.reduce()
+    F32.close()
+    F64 = pf.PhaseField(m, pf.PF_PREC_FP64)
+    F64.upload(st, 0.0)
+    F64.update(S)
+    a64 = F64.download(conc=False)
+    F64.close()
+    A = pf.Adjoint(m, pf.PF_PREC_FP64, max(S, 1))
+    A.upload(st, 0.0)
+    A.forward(S)
+    a4 = A.final_state()
+    A.close()
+
+    def err(ref_phase, ref_C):
+        d = np.abs(a32["phase"] - ref_phase)
+        fr32 = a32["phase"].reshape(N, 3).mean(0)
+        frr = ref_phase.reshape(N, 3).mean(0)
+        return {"phase_max_abs": float(d.max()), "phase_mean_abs": float(d.mean()),
+                "cells_phase_err_gt_1e-5": int((d.reshape(N, 3).max(1) > 1e-5).sum()),
+                "carbon_max_rel": float(np.max(np.abs(a32["C"][:N] - ref_C) / np.abs(ref_C))),
+                "phase_fraction_abs": [float(x) for x in np.abs(fr32 - frr)]}
+
+    C0 = st["C"][:N].sum()
+    return {"grid": list(grid), "steps": S, "cells": N,
+            "vs_fp64_four_slot": err(a4["phase"], a4["C"]),
+            "vs_fp64_six_slot": err(a64["phase"], a64["C"][:N]),
+            "carbon_mass_rel_drift_fp32": float(abs(r32[4] - C0) / C0)}
+
+
 def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     import numpy as np
     import torch
@@ -463,6 +512,7 @@ def main() -> None:
     ap.add_argument("--no-tune", action="store_true", help="skip the diffusion tile autotuner")
     ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-domain ensemble (0 = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint calibration run (0 = skip)")
+    ap.add_argument("--precision-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 error run (0 = skip)")
     ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -493,6 +543,8 @@ def main() -> None:
             out["batch"] = b
     if args.adjoint_steps > 0 and out is not None:
         out["adjoint"] = run_adjoint(args)
+    if args.precision_steps > 0 and out is not None:
+        out["precision"] = run_precision(args)
     if out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -244,6 +244,9 @@ int pf_adj_set_scales(pf_adj *a, const double scales[4]);
 int pf_adj_forward(pf_adj *a, int nsteps, double J[2]);
 int pf_adj_gradient(pf_adj *a, int objective, double grad[4]);
 int pf_adj_timings(pf_adj *a, double ms[2]);
+/* Phase fractions [N*3] and total carbon [N] at the end of the last forward run
+ * (the four-slot model: the FP64 reference for the FP32 compact path). */
+int pf_adj_final_state(pf_adj *a, double *phase, double *C);
 int pf_adj_destroy(pf_adj *a);
 
 /* Reference output writers (write_data.cpp:3-82).  pf_write_data appends a

@@ -154,6 +154,7 @@ SYMBOLS = {
     "pf_adj_forward": (_I, [_P, _I, _DP]),
     "pf_adj_gradient": (_I, [_P, _I, _DP]),
     "pf_adj_timings": (_I, [_P, _DP]),
+    "pf_adj_final_state": (_I, [_P, _DP, _DP]),
     "pf_adj_destroy": (_I, [_P]),
 }
 
@@ -440,6 +441,12 @@ class Adjoint:
         g = np.zeros(4, np.float64)
         check(lib().pf_adj_gradient(self._a, objective, g.ctypes.data_as(_DP)), "pf_adj_gradient")
         return g
+
+    def final_state(self) -> dict:
+        N = self.model.ix * self.model.iy * self.model.iz
+        ph, C = np.zeros(3 * N), np.zeros(N)
+        check(lib().pf_adj_final_state(self._a, ph.ctypes.data_as(_DP), C.ctypes.data_as(_DP)), "pf_adj_final_state")
+        return {"phase": ph, "C": C}
 
     def timings(self) -> dict:
         t = np.zeros(2, np.float64)

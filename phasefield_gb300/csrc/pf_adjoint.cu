@@ -516,6 +516,7 @@ struct AdjCtx : pf_adj_impl {
     cudaGraphExec_t fwd_graph[2] = {nullptr, nullptr};
     cudaGraphExec_t seg_graph = nullptr;
     R *g_C = nullptr, *g_phi = nullptr, *g_ph = nullptr;  // adjoint buffer roles at capture
+    const R *fin_ph = nullptr, *fin_C = nullptr;            // final state of the last forward run
 
     void drop_graphs() {
         for (auto &g : fwd_graph)
@@ -793,6 +794,8 @@ static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
     }
     cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
     AP<R> P = c->P;
+    c->fin_ph = ha;
+    c->fin_C = Ca;
     k_objective_sums<R><<<256, 256, 0, c->s>>>(P, ha, Ca, c->d_acc);
     double h[8];
     cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
@@ -946,6 +949,24 @@ extern "C" int pf_adj_gradient(pf_adj *a, int objective, double grad[4]) {
     if (!a || !grad || objective < 0 || objective > 1) return pf_fail(PF_ERR_ARG, "pf_adj_gradient: bad arguments");
     return a->prec == PF_PREC_FP64 ? adj_gradient(as<double>(a), objective, grad)
                                    : adj_gradient(as<float>(a), objective, grad);
+}
+
+template <typename R>
+static int adj_final(AdjCtx<R> *c, double *phase, double *C) {
+    if (!c->have_fwd || !c->fin_ph) return pf_fail(PF_ERR_ARG, "pf_adj_final_state: run pf_adj_forward first");
+    const size_t N = (size_t)c->N;
+    std::vector<R> h(3 * N), hc(N);
+    cudaMemcpyAsync(h.data(), c->fin_ph, 3 * N * sizeof(R), cudaMemcpyDeviceToHost, c->s);
+    cudaMemcpyAsync(hc.data(), c->fin_C, N * sizeof(R), cudaMemcpyDeviceToHost, c->s);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_final_state failed");
+    for (size_t i = 0; i < 3 * N; i++) phase[i] = (double)h[i];
+    for (size_t i = 0; i < N; i++) C[i] = (double)hc[i];
+    return PF_OK;
+}
+
+extern "C" int pf_adj_final_state(pf_adj *a, double *phase, double *C) {
+    if (!a || !phase || !C) return pf_fail(PF_ERR_ARG, "pf_adj_final_state: null argument");
+    return a->prec == PF_PREC_FP64 ? adj_final(as<double>(a), phase, C) : adj_final(as<float>(a), phase, C);
 }
 
 extern "C" int pf_adj_timings(pf_adj *a, double ms[2]) {
