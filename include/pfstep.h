@@ -201,6 +201,12 @@ int pf_use_graph(pf_ctx *ctx, int on);
  * chosen tile height, z chunk, kernel variant (0: two barriers per plane, 1:
  * double-buffered records) and mean launch time.  No-op for FP64. */
 int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *variant, float *ms);
+/* Fix the FP32C diffusion tile shape (tile_y 4/8/16, z chunk, variant 0/1);
+ * tile_y = 0 returns to the default rule. */
+int pf_set_diffusion_tile(pf_ctx *ctx, int tile_y, int zchunk, int variant);
+/* The autotuner's candidates as (tile_y, zchunk, variant) triples; returns
+ * how many were written (at most max). */
+int pf_diffusion_candidates(pf_ctx *ctx, int *out, int max);
 /* Batched ensemble (no reference counterpart): many independent 2D domains
  * (own size, constant temperature, time step, sub-step count), each stored
  * like a PF_PREC_FP32C context, advanced together by one persistent

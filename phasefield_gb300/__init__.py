@@ -137,6 +137,8 @@ SYMBOLS = {
     "pf_use_graph": (_I, [_P, _I]),
     "pf_autotune": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                          ctypes.POINTER(ctypes.c_float)]),
+    "pf_set_diffusion_tile": (_I, [_P, _I, _I, _I]),
+    "pf_diffusion_candidates": (_I, [_P, ctypes.POINTER(_I), _I]),
     "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
     "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
     "pf_reduce_noalloc": (_I, [ctypes.c_longlong, _I, _P, _P, _P, _P, _P, _P]),
@@ -329,6 +331,16 @@ class PhaseField:
         check(lib().pf_autotune(self._ctx, ctypes.byref(ty), ctypes.byref(zc), ctypes.byref(d), ctypes.byref(ms)),
               "pf_autotune")
         return {"tile_y": ty.value, "zchunk": zc.value, "variant": d.value, "ms": ms.value}
+
+    def set_diffusion_tile(self, tile_y: int, zchunk: int, variant: int) -> None:
+        check(lib().pf_set_diffusion_tile(self._ctx, tile_y, zchunk, variant), "pf_set_diffusion_tile")
+
+    def diffusion_candidates(self) -> list:
+        buf = (ctypes.c_int * 192)()
+        n = lib().pf_diffusion_candidates(self._ctx, buf, 64)
+        if n < 0:
+            check(n, "pf_diffusion_candidates")
+        return [(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]) for i in range(n)]
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(lib().pf_set_stream(self._ctx, ctypes.c_void_p(stream_handle) if stream_handle else None),

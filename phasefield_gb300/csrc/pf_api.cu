@@ -608,6 +608,37 @@ extern "C" int pf_autotune(pf_ctx *c, int *ty, int *zchunk, int *variant, float 
     return PF_OK;
 }
 
+extern "C" int pf_set_diffusion_tile(pf_ctx *c, int ty, int zchunk, int variant) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_set_diffusion_tile: null context");
+    if (ty == 0) {  // back to the default rule
+        c->diff_cfg_valid = false;
+        return PF_OK;
+    }
+    if ((ty != 4 && ty != 8 && ty != 16) || zchunk < 1 || variant < 0 || variant > 1)
+        return pf_fail(PF_ERR_ARG, "pf_set_diffusion_tile: tile height 4/8/16, z chunk >= 1, variant 0/1");
+    c->diff_cfg = pf_diff_cfg{ty, zchunk, variant};
+    c->diff_cfg_valid = true;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    return PF_OK;
+}
+
+extern "C" int pf_diffusion_candidates(pf_ctx *c, int *out, int max) {
+    if (!c || !out) return pf_fail(PF_ERR_ARG, "pf_diffusion_candidates: null argument");
+    pf_step_params P;
+    pf_compute_params(c->model, c->time, P);
+    pf_f32_params F;
+    pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
+    pf_diff_cfg cand[64];
+    const int n = pf_diffuse_candidates(F, cand, 64);
+    int k = 0;
+    for (int i = 0; i < n && k < max; i++, k++) {
+        out[3 * k] = cand[i].ty;
+        out[3 * k + 1] = cand[i].zchunk;
+        out[3 * k + 2] = cand[i].variant;
+    }
+    return k;
+}
+
 extern "C" int pf_reduce(pf_ctx *c, double out[8]) {
     if (!c || !c->have_state || !out) return pf_fail(PF_ERR_ARG, "pf_reduce: no state");
     cudaError_t e;

@@ -79,10 +79,9 @@ __device__ __forceinline__ void derive(const pf_f32_params &P, const float s[3],
     for (int q = 0; q < NSOL; q++) pf_partition_q(P, q, C[q], ph, d.c[q]);
 }
 
-// Raw data is prefetched two planes ahead (three stages).  DB: the derived
-// records are double-buffered by plane parity, which saves the second barrier
-// of every plane at the cost of shared memory (3 instead of 4 resident blocks).
-template <int NSOL, int TX, int TY, bool DB>
+// Variant 0.  Raw data is prefetched two planes ahead (three stages); the
+// first NH threads also stage and derive the tile's halo cells.
+template <int NSOL, int TX, int TY>
 struct Smem {
     static constexpr int NT = TX * TY, NH = 2 * TX + 2 * TY, W = TX + 2, H = TY + 2, NST = 3;
     using SV = typename Vec<NSOL>::T;
@@ -90,15 +89,15 @@ struct Smem {
     SV hso[NST][NH];      // raw solute totals, halo cells
     float sp[NST][3][NT];  // raw s_p, own cells
     float hsp[NST][3][NH]; // raw s_p, halo cells
-    SV rec[DB ? 2 : 1][3][H][W];  // derived records of the current plane, with halo
+    SV rec[3][H][W];      // derived records of the current plane, with halo
 };
 
-template <int NSOL, int NNB, int TX, int TY, bool DB>
-__global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffuse(const __grid_constant__ pf_f32_params P,
+template <int NSOL, int NNB, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __grid_constant__ pf_f32_params P,
                                                                      const float *__restrict__ sphase,
                                                                      const float2 *__restrict__ sol_in,
                                                                      float2 *__restrict__ sol_out, int zchunk) {
-    using S = Smem<NSOL, TX, TY, DB>;
+    using S = Smem<NSOL, TX, TY>;
     using SV = typename Vec<NSOL>::T;
     static_assert(S::NH <= S::NT, "halo needs one thread per halo cell");
     constexpr bool use_y = NNB >= 4, use_z = NNB >= 6;
@@ -168,13 +167,12 @@ __global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffu
     auto body = [&](int z, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
         issue(z + 2);
         cp_wait<1>();  // planes z (halo) and z+1 (own) have landed
-        const int rb = DB ? (z & 1) : 0;
 #pragma unroll
         for (int p = 0; p < 3; p++) {
             float cp[NSOL];
 #pragma unroll
             for (int q = 0; q < NSOL; q++) cp[q] = cur.c[q][p];
-            sm.rec[rb][p][ly + 1][lx + 1] = pack_rec<NSOL>(cur.s[p], cp);
+            sm.rec[p][ly + 1][lx + 1] = pack_rec<NSOL>(cur.s[p], cp);
         }
         if (has_halo) {
             const int st = stage(z);
@@ -188,7 +186,7 @@ __global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffu
                 float cp[NSOL];
 #pragma unroll
                 for (int q = 0; q < NSOL; q++) cp[q] = dh.c[q][p];
-                sm.rec[rb][p][hy + 1][hx + 1] = pack_rec<NSOL>(dh.s[p], cp);
+                sm.rec[p][hy + 1][hx + 1] = pack_rec<NSOL>(dh.s[p], cp);
             }
         }
         __syncthreads();
@@ -196,9 +194,9 @@ __global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffu
         float acc[NSOL][3];
 #pragma unroll
         for (int p = 0; p < 3; p++) {
-            const SV l = sm.rec[rb][p][ly + 1][lx], r = sm.rec[rb][p][ly + 1][lx + 2];
+            const SV l = sm.rec[p][ly + 1][lx], r = sm.rec[p][ly + 1][lx + 2];
             SV d, u;
-            if (use_y) { d = sm.rec[rb][p][ly][lx + 1]; u = sm.rec[rb][p][ly + 2][lx + 1]; }
+            if (use_y) { d = sm.rec[p][ly][lx + 1]; u = sm.rec[p][ly + 2][lx + 1]; }
 #pragma unroll
             for (int q = 0; q < NSOL; q++) {
                 const float c0 = cur.c[q][p];
@@ -232,7 +230,7 @@ __global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffu
             if (NSOL == 2) reinterpret_cast<float4 *>(sol_out)[n] = make_float4(o[0], o[1], o[2], o[2 * NSOL - 1]);
             else sol_out[n] = make_float2(o[0], o[1]);
         }
-        if (!DB) __syncthreads();
+        __syncthreads();
     };
 
     Der<NSOL> A, B, Cd;
@@ -248,21 +246,181 @@ __global__ void __launch_bounds__(TX *TY, (DB ? 768 : 1024) / (TX * TY)) k_diffu
     }
 }
 
-template <int NSOL, int NNB, int TY, bool DB>
+// ---------------------------------------------------------------------------
+// Variant 1: halo warps.  A block holds TY interior warps (one 32-cell row of
+// the tile each) and three halo warps: the row above, the row below, and the
+// two halo columns (lanes 0..TY-1 and TY..2TY-1).  Every thread owns one cell
+// column of the tile with its halo, stages that column's raw data and forms
+// that column's derived record for every plane, so each warp does exactly one
+// batch of derived records per plane and no warp waits at the barrier for
+// another's halo work.  Only interior threads compute fluxes.
+// ---------------------------------------------------------------------------
+template <int NSOL, int TY>
+struct SmemHW {
+    static constexpr int TX = 32, NT = 32 * (TY + 3), W = TX + 2, H = TY + 2, NST = 3;
+    using SV = typename Vec<NSOL>::T;
+    SV so[NST][NT];
+    float sp[NST][3][NT];
+    SV rec[3][H][W];
+};
+
+template <int NSOL, int NNB, int TY>
+__global__ void __launch_bounds__(32 * (TY + 3), (TY <= 4 ? 4 : (TY <= 8 ? 2 : 1)))
+    k_diffuse_hw(const __grid_constant__ pf_f32_params P, const float *__restrict__ sphase,
+                 const float2 *__restrict__ sol_in, float2 *__restrict__ sol_out, int zchunk) {
+    using S = SmemHW<NSOL, TY>;
+    using SV = typename Vec<NSOL>::T;
+    constexpr int TX = S::TX;
+    constexpr bool use_y = NNB >= 4, use_z = NNB >= 6;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S &sm = *reinterpret_cast<S *>(smem_raw);
+
+    const int ix = P.ix, iy = P.iy, iz = P.iz;
+    const long long N = P.N;
+    const long long plane = (long long)ix * iy;
+    const int tiles_x = (ix + TX - 1) / TX;
+    const int tx0 = (int)(blockIdx.x % tiles_x) * TX;
+    const int ty0 = (int)(blockIdx.x / tiles_x) * TY;
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+    int sx = 0, sy = 0;  // slot in the record tile
+    bool active = true;
+    if (w < TY) { sx = l + 1; sy = w + 1; }
+    else if (w == TY) { sx = l + 1; sy = 0; }
+    else if (w == TY + 1) { sx = l + 1; sy = TY + 1; }
+    else if (l < TY) { sx = 0; sy = l + 1; }
+    else if (l < 2 * TY) { sx = TX + 1; sy = l - TY + 1; }
+    else active = false;
+    const bool interior = w < TY;
+    const bool valid = interior && (tx0 + l < ix) && (ty0 + w < iy);
+    const long long col = pf_mod(tx0 + sx - 1, ix) + (long long)ix * pf_mod(ty0 + sy - 1, iy);
+    const int z0 = blockIdx.y * zchunk;
+    const int z1 = min(z0 + zchunk, iz);
+    const int zlo = use_z ? z0 - 1 : z0, zhi = use_z ? z1 : z1 - 1;
+    const SV *own_v = reinterpret_cast<const SV *>(sol_in) + col;
+    const float *own_s = sphase + col;
+
+    auto stage = [&](int zz) { return (zz - zlo) % S::NST; };
+    auto issue = [&](int zz) {
+        if (active && zz >= zlo && zz <= zhi) {
+            const int st = stage(zz);
+            const long long off = plane * pf_mod(zz, iz);
+            cp_async4(&sm.sp[st][0][tid], own_s + off);
+            cp_async4(&sm.sp[st][1][tid], own_s + N + off);
+            cp_async4(&sm.sp[st][2][tid], own_s + 2 * N + off);
+            if (NSOL == 2) cp_async16(&sm.so[st][tid], own_v + off);
+            else cp_async8(&sm.so[st][tid], own_v + off);
+        }
+        cp_commit();
+    };
+    auto derive_own = [&](int zz, Der<NSOL> &d) {
+        const int st = stage(zz);
+        const float s3[3] = {sm.sp[st][0][tid], sm.sp[st][1][tid], sm.sp[st][2][tid]};
+        float C[NSOL], comp[NSOL];
+        unpack_sol<NSOL>(sm.so[st][tid], C, comp);
+        derive<NSOL>(P, s3, C, d);
+    };
+    auto body = [&](int z, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
+        issue(z + 2);
+        cp_wait<1>();
+        if (active) {
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                float cp[NSOL];
+#pragma unroll
+                for (int q = 0; q < NSOL; q++) cp[q] = cur.c[q][p];
+                sm.rec[p][sy][sx] = pack_rec<NSOL>(cur.s[p], cp);
+            }
+        }
+        __syncthreads();
+        if (active && z + 1 <= zhi) derive_own(z + 1, next);
+        if (valid) {
+            float acc[NSOL][3];
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                const SV lr = sm.rec[p][sy][sx - 1], rr = sm.rec[p][sy][sx + 1];
+                SV d, u;
+                if (use_y) { d = sm.rec[p][sy - 1][sx]; u = sm.rec[p][sy + 1][sx]; }
+#pragma unroll
+                for (int q = 0; q < NSOL; q++) {
+                    const float c0 = cur.c[q][p];
+                    float a = lr.x * (rec_c(lr, q) - c0);
+                    a += rr.x * (rec_c(rr, q) - c0);
+                    if (use_y) {
+                        a += d.x * (rec_c(d, q) - c0);
+                        a += u.x * (rec_c(u, q) - c0);
+                    }
+                    if (use_z) {
+                        a += prev.s[p] * (prev.c[q][p] - c0);
+                        a += next.s[p] * (next.c[q][p] - c0);
+                    }
+                    acc[q][p] = a;
+                }
+            }
+            float C[NSOL], comp[NSOL];
+            unpack_sol<NSOL>(sm.so[stage(z)][tid], C, comp);
+            float o[2 * NSOL];
+#pragma unroll
+            for (int q = 0; q < NSOL; q++) {
+                const float flux = cur.s[0] * P.D[q][0] * acc[q][0] + cur.s[1] * P.D[q][1] * acc[q][1] +
+                                   cur.s[2] * P.D[q][2] * acc[q][2];
+                const float y = flux - comp[q];
+                const float t = C[q] + y;
+                o[2 * q] = t;
+                o[2 * q + 1] = (t - C[q]) - y;
+            }
+            const long long n = col + plane * z;
+            if (NSOL == 2) reinterpret_cast<float4 *>(sol_out)[n] = make_float4(o[0], o[1], o[2], o[2 * NSOL - 1]);
+            else sol_out[n] = make_float2(o[0], o[1]);
+        }
+        __syncthreads();
+    };
+
+    Der<NSOL> A, B, Cd;
+    for (int zz = zlo; zz <= z0 + 1; zz++) issue(zz);
+    cp_wait<1>();
+    if (active) {
+        if (use_z) derive_own(z0 - 1, A);
+        derive_own(z0, B);
+    }
+    for (int z = z0; z < z1; z += 3) {
+        body(z, A, B, Cd);
+        if (z + 1 < z1) body(z + 1, B, Cd, A);
+        if (z + 2 < z1) body(z + 2, Cd, A, B);
+    }
+}
+
+template <int NSOL, int NNB, int TY>
+cudaError_t launch_hw(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
+                      cudaStream_t s, int zchunk) {
+    using S = SmemHW<NSOL, TY>;
+    const int tiles = ((P.ix + 31) / 32) * ((P.iy + TY - 1) / TY);
+    const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_diffuse_hw<NSOL, NNB, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(S));
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    k_diffuse_hw<NSOL, NNB, TY><<<grid, S::NT, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
+    return cudaGetLastError();
+}
+
+template <int NSOL, int NNB, int TY>
 cudaError_t launch_one(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
                        cudaStream_t s, int zchunk) {
     constexpr int TX = 32;
-    using S = Smem<NSOL, TX, TY, DB>;
+    using S = Smem<NSOL, TX, TY>;
     const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY, DB>,
+        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    k_diffuse<NSOL, NNB, TX, TY, DB><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
+    k_diffuse<NSOL, NNB, TX, TY><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
 }
 
@@ -271,15 +429,15 @@ cudaError_t launch_ty(const pf_f32_params &P, const float *sphase, const float2 
                       cudaStream_t s, int ty, int zchunk, int variant) {
     if (variant == 1) {
         switch (ty) {
-            case 4: return launch_one<NSOL, NNB, 4, true>(P, sphase, sol_in, sol_out, s, zchunk);
-            case 16: return launch_one<NSOL, NNB, 16, true>(P, sphase, sol_in, sol_out, s, zchunk);
-            default: return launch_one<NSOL, NNB, 8, true>(P, sphase, sol_in, sol_out, s, zchunk);
+            case 4: return launch_hw<NSOL, NNB, 4>(P, sphase, sol_in, sol_out, s, zchunk);
+            case 16: return launch_hw<NSOL, NNB, 16>(P, sphase, sol_in, sol_out, s, zchunk);
+            default: return launch_hw<NSOL, NNB, 8>(P, sphase, sol_in, sol_out, s, zchunk);
         }
     }
     switch (ty) {
-        case 4: return launch_one<NSOL, NNB, 4, false>(P, sphase, sol_in, sol_out, s, zchunk);
-        case 16: return launch_one<NSOL, NNB, 16, false>(P, sphase, sol_in, sol_out, s, zchunk);
-        default: return launch_one<NSOL, NNB, 8, false>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 4: return launch_one<NSOL, NNB, 4>(P, sphase, sol_in, sol_out, s, zchunk);
+        case 16: return launch_one<NSOL, NNB, 16>(P, sphase, sol_in, sol_out, s, zchunk);
+        default: return launch_one<NSOL, NNB, 8>(P, sphase, sol_in, sol_out, s, zchunk);
     }
 }
 

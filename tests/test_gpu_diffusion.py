@@ -47,6 +47,29 @@ def test_diffusion_fp64_matches_oracle(gpu, tmp_path, grid):
     assert np.array_equal(got["conc"], ref["conc"])
 
 
+@pytest.mark.parametrize("grid", [(64, 40, 33), (37, 23, 1), (48, 1, 20)])
+def test_every_tile_candidate_gives_the_same_answer(gpu, tmp_path, grid):
+    """Each tile shape / kernel variant the autotuner may pick, against FP64."""
+    m, om, spec = small_case(str(tmp_path), "3d256", grid, n_grains=5, n_nuclei=6, radius=2.0, noise=(0.02, 0.02))
+    st0 = pf.init_microstructure(m, spec, 0.0)
+    F64 = pf.PhaseField(m, pf.PF_PREC_FP64)
+    F64.upload(st0, 0.0)
+    F64.diffuse(6)
+    ref = F64.download()
+    N = m.ix * m.iy * m.iz
+    F = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    F.upload(st0, 0.0)
+    cands = F.diffusion_candidates()
+    assert {c[2] for c in cands} == {0, 1}
+    for ty, zc, var in cands:
+        F.upload(st0, 0.0)
+        F.set_diffusion_tile(ty, zc, var)
+        F.diffuse(6)
+        got = F.download()
+        err = rel_maxnorm(got["C"][:N], ref["C"][:N])
+        assert err <= 2e-6, (ty, zc, var, err)
+
+
 @pytest.mark.parametrize("grid", GRIDS)
 def test_diffusion_fp32_tracks_fp64(gpu, tmp_path, grid):
     m, om, spec = small_case(str(tmp_path), "3d256", grid, n_grains=5, n_nuclei=6, radius=2.0, noise=(0.02, 0.02))
