@@ -76,6 +76,31 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     const float4 v = pf_ld<CG>(phi1 + n);
     const int oid[4] = {g.x, g.y, g.z, g.w};
     const float ov[4] = {v.x, v.y, v.z, v.w};
+    long long nb[6];
+    nb[0] = n - i + pf_wrap(i, ix, -1);
+    nb[1] = n - i + pf_wrap(i, ix, 1);
+    nb[2] = n + (long long)ix * (pf_wrap(j, iy, -1) - j);
+    nb[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
+    nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
+    nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
+    // Fast path for the common bulk cell: one grain above the cutoff here and
+    // the same single grain (and nothing else) in every neighbour -- the merged
+    // stencil list would hold one entry (solver.cpp:207-216), so copy.
+    if (g.y == 0 && g.z == 0 && g.w == 0 && v.x > cutoff) {
+        bool bulk = true;
+#pragma unroll
+        for (int b = 0; b < 6; b++) {
+            if (b < P.nnb) {
+                const ushort4 ng = pf_ld<CG>(gid1 + nb[b]);
+                bulk = bulk && ng.x == g.x && ng.y == 0;
+            }
+        }
+        if (bulk) {
+            gid2[n] = g;
+            phi2[n] = v;
+            return;
+        }
+    }
     // solver.cpp:168-177: own slots above the cutoff (a sorted prefix).
     int num = 0;
 #pragma unroll
@@ -89,13 +114,6 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     }
     // solver.cpp:179-205: merge the neighbours' lists (x-, x+, y-, y+, z-, z+),
     // each scanned until its first empty slot.
-    long long nb[6];
-    nb[0] = n - i + pf_wrap(i, ix, -1);
-    nb[1] = n - i + pf_wrap(i, ix, 1);
-    nb[2] = n + (long long)ix * (pf_wrap(j, iy, -1) - j);
-    nb[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
-    nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
-    nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
 #pragma unroll
     for (int b = 0; b < 6; b++) {
         if (b < P.nnb) {

@@ -72,35 +72,56 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce_f32(long long N, int nso
                                                             const float *__restrict__ phase,
                                                             const float2 *__restrict__ sol,
                                                             double *__restrict__ partials) {
-    double acc[PF_RED_NOUT] = {0., 0., 0., 0., 0., 0., 0., 0.};
+    // Each thread sums its few dozen cells in FP32 with Kahan compensation
+    // (error ~ eps^2 of the partial), then the partials go to FP64: the sums
+    // keep FP64 accuracy without per-cell FP64 arithmetic.
+    float s[9], c[9];
+#pragma unroll
+    for (int o = 0; o < 9; o++) { s[o] = 0.f; c[o] = 0.f; }
+    auto kadd = [&](int o, float v) {
+        const float y = v - c[o];
+        const float t = s[o] + y;
+        c[o] = (t - s[o]) - y;
+        s[o] = t;
+    };
+    int bad = 0;
     for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x; n < N;
          n += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int p = 0; p < 3; p++) {
-            const double sq = (double)phase[p * N + n];  // planes hold sqrt(phase fraction)
-            const double v = sq * sq;
-            acc[p] += v;
-            acc[7] += nf(v);
+            const float sq = phase[p * N + n];  // planes hold sqrt(phase fraction)
+            bad += !isfinite(sq);
+            kadd(p, sq * sq);
         }
         const ushort4 g = gid[n];
         const float4 v4 = phi[n];
         const int l[4] = {g.x, g.y, g.z, g.w};
         const float fv[4] = {v4.x, v4.y, v4.z, v4.w};
+        float def = 0.f;
 #pragma unroll
         for (int a = 0; a < 4; a++) {
-            acc[3] += (l[a] <= deformed_max_local) ? (double)fv[a] : 0.;
-            acc[7] += nf((double)fv[a]);
+            bad += !isfinite(fv[a]);
+            def += (l[a] <= deformed_max_local) ? fv[a] : 0.f;
         }
+        kadd(3, def);
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             if (q < nsol) {
-                const float2 s = sol[n * nsol + q];
-                const double v = (double)s.x - (double)s.y;
-                acc[4 + q] += v;
-                acc[7] += nf(v);
+                const float2 v = sol[n * nsol + q];
+                bad += !isfinite(v.x) + !isfinite(v.y);
+                kadd(4 + q, v.x);
+                kadd(6 + q, v.y);
             }
         }
     }
+    double acc[PF_RED_NOUT];
+#pragma unroll
+    for (int o = 0; o < 4; o++) acc[o] = (double)s[o] - (double)c[o];
+    // Solute totals: true value = sum(x) - sum(compensation).
+    acc[4] = ((double)s[4] - (double)c[4]) - ((double)s[6] - (double)c[6]);
+    acc[5] = ((double)s[5] - (double)c[5]) - ((double)s[7] - (double)c[7]);
+    acc[6] = 0.;
+    acc[7] = (double)bad;
     block_store_partials(acc, partials + (long long)blockIdx.x * PF_RED_NOUT);
 }
 
