@@ -86,15 +86,15 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     // Fast path for the common bulk cell: one grain above the cutoff here and
     // the same single grain (and nothing else) in every neighbour -- the merged
     // stencil list would hold one entry (solver.cpp:207-216), so copy.
+    ushort4 ngid[6];
+#pragma unroll
+    for (int b = 0; b < 6; b++)
+        if (b < P.nnb) ngid[b] = pf_ld<CG>(gid1 + nb[b]);
     if (g.y == 0 && g.z == 0 && g.w == 0 && v.x > cutoff) {
         bool bulk = true;
 #pragma unroll
-        for (int b = 0; b < 6; b++) {
-            if (b < P.nnb) {
-                const ushort4 ng = pf_ld<CG>(gid1 + nb[b]);
-                bulk = bulk && ng.x == g.x && ng.y == 0;
-            }
-        }
+        for (int b = 0; b < 6; b++)
+            if (b < P.nnb) bulk = bulk && ngid[b].x == g.x && ngid[b].y == 0;
         if (bulk) {
             gid2[n] = g;
             phi2[n] = v;
@@ -117,7 +117,7 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
 #pragma unroll
     for (int b = 0; b < 6; b++) {
         if (b < P.nnb) {
-            const ushort4 ng = pf_ld<CG>(gid1 + nb[b]);
+            const ushort4 ng = ngid[b];
             const float4 nv4 = pf_ld<CG>(phi1 + nb[b]);
             const int nid[4] = {ng.x, ng.y, ng.z, ng.w};
             const float nv[4] = {nv4.x, nv4.y, nv4.z, nv4.w};
