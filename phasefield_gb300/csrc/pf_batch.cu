@@ -160,7 +160,7 @@ __device__ __forceinline__ void diffuse_tile(const pf_f32_params &P, int tx0, in
 }
 
 template <int NSOL>
-__global__ void __launch_bounds__(kBT) k_batch(const pf_batch_dom *__restrict__ doms,
+__global__ void __launch_bounds__(kBT, 4) k_batch(const pf_batch_dom *__restrict__ doms,
                                                const pf_f32_params *__restrict__ params,
                                                const int *__restrict__ block_dom, int nsteps,
                                                unsigned long long *ctr, int *err, unsigned long long timeout_ns) {
