@@ -19,6 +19,7 @@
 //   registers, rotated without copies by a three-way unrolled z loop.
 // * The solute total is advanced with a Kahan-compensated sum.  D carries
 //   dt_sub/dx^2.
+#include <type_traits>
 #include "pf_f32.cuh"
 #include "pf_kernels.h"
 
@@ -135,11 +136,14 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     const SV *own_v = solv + col;
     const SV *halo_v = solv + hcol;
 
-    auto stage = [&](int zz) { return (zz - zlo) % S::NST; };
-    auto issue = [&](int zz) {
+    // Plane zz lives in stage (zz - zlo) % 3.  Every call site below knows that
+    // stage at compile time: the z loop is unrolled by three and zlo - z0 is
+    // fixed by use_z, so no integer division appears in the loop.
+    constexpr int OFF = use_z ? 1 : 0;  // z0 - zlo
+    auto issue = [&](int zz, int st) {
         if (zz >= zlo && zz <= zhi) {
-            const int st = stage(zz);
-            const long long off = plane * pf_mod(zz, iz);
+            const int zw = zz < 0 ? zz + iz : (zz >= iz ? zz - iz : zz);  // |wrap| <= 1 plane
+            const long long off = plane * zw;
             cp_async4(&sm.sp[st][0][tid], own_s + off);
             cp_async4(&sm.sp[st][1][tid], own_s + N + off);
             cp_async4(&sm.sp[st][2][tid], own_s + 2 * N + off);
@@ -155,17 +159,19 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
         }
         cp_commit();
     };
-    auto derive_own = [&](int zz, Der<NSOL> &d) {
-        const int st = stage(zz);
+    auto derive_own = [&](int st, Der<NSOL> &d) {
         const float s3[3] = {sm.sp[st][0][tid], sm.sp[st][1][tid], sm.sp[st][2][tid]};
         float C[NSOL], comp[NSOL];
         unpack_sol<NSOL>(sm.so[st][tid], C, comp);
         derive<NSOL>(P, s3, C, d);
     };
 
-    // One plane.  prev/cur/next rotate through the unrolled loop below.
-    auto body = [&](int z, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
-        issue(z + 2);
+    // One plane; J is the position in the three-way unrolled loop, so the
+    // stages of planes z, z+1, z+2 are constants.  prev/cur/next rotate.
+    auto body = [&](int z, auto J, const Der<NSOL> &prev, const Der<NSOL> &cur, Der<NSOL> &next) {
+        constexpr int j = decltype(J)::value;
+        constexpr int st_z = (OFF + j) % 3, st_z1 = (OFF + j + 1) % 3, st_z2 = (OFF + j + 2) % 3;
+        issue(z + 2, st_z2);
         cp_wait<1>();  // planes z (halo) and z+1 (own) have landed
 #pragma unroll
         for (int p = 0; p < 3; p++) {
@@ -175,10 +181,9 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
             sm.rec[p][ly + 1][lx + 1] = pack_rec<NSOL>(cur.s[p], cp);
         }
         if (has_halo) {
-            const int st = stage(z);
-            const float s3[3] = {sm.hsp[st][0][hid], sm.hsp[st][1][hid], sm.hsp[st][2][hid]};
+            const float s3[3] = {sm.hsp[st_z][0][hid], sm.hsp[st_z][1][hid], sm.hsp[st_z][2][hid]};
             float C[NSOL], comp[NSOL];
-            unpack_sol<NSOL>(sm.hso[st][hid], C, comp);
+            unpack_sol<NSOL>(sm.hso[st_z][hid], C, comp);
             Der<NSOL> dh;
             derive<NSOL>(P, s3, C, dh);
 #pragma unroll
@@ -190,7 +195,7 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
             }
         }
         __syncthreads();
-        if (z + 1 <= zhi) derive_own(z + 1, next);
+        if (z + 1 <= zhi) derive_own(st_z1, next);
         float acc[NSOL][3];
 #pragma unroll
         for (int p = 0; p < 3; p++) {
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
         }
         if (valid) {
             float C[NSOL], comp[NSOL];
-            unpack_sol<NSOL>(sm.so[stage(z)][tid], C, comp);
+            unpack_sol<NSOL>(sm.so[st_z][tid], C, comp);
             float o[2 * NSOL];
 #pragma unroll
             for (int q = 0; q < NSOL; q++) {
@@ -234,15 +239,17 @@ __global__ void __launch_bounds__(TX *TY, 1024 / (TX * TY)) k_diffuse(const __gr
     };
 
     Der<NSOL> A, B, Cd;
-    // Planes zlo .. z0+1 in flight; zlo and z0 must have landed.
-    for (int zz = zlo; zz <= z0 + 1; zz++) issue(zz);
+    // Planes zlo .. z0+1 in flight (stages 0, 1[, 2]); zlo and z0 must have landed.
+    issue(zlo, 0);
+    issue(zlo + 1, 1);
+    if (use_z) issue(zlo + 2, 2);
     cp_wait<1>();
-    if (use_z) derive_own(z0 - 1, A);
-    derive_own(z0, B);
+    if (use_z) derive_own(0, A);
+    derive_own(OFF, B);
     for (int z = z0; z < z1; z += 3) {
-        body(z, A, B, Cd);
-        if (z + 1 < z1) body(z + 1, B, Cd, A);
-        if (z + 2 < z1) body(z + 2, Cd, A, B);
+        body(z, std::integral_constant<int, 0>{}, A, B, Cd);
+        if (z + 1 < z1) body(z + 1, std::integral_constant<int, 1>{}, B, Cd, A);
+        if (z + 2 < z1) body(z + 2, std::integral_constant<int, 2>{}, Cd, A, B);
     }
 }
 
