@@ -185,6 +185,11 @@ int pf_diffuse(pf_ctx *ctx, int nsub);
  * phi over slots with grain id < 100000, out[4..5] solute totals, out[6] 0,
  * out[7] count of non-finite values.  Divide by N for write_data.cpp:14-18. */
 int pf_reduce(pf_ctx *ctx, double out[8]);
+/* Failure check on the FP64 statistics: PF_ERR_NONFINITE if any value of the
+ * state is NaN/Inf, or if a solute total differs from reference_totals[q] by
+ * more than max_rel_drift (relative; skipped when reference_totals is NULL or
+ * max_rel_drift <= 0).  out (may be NULL) receives the pf_reduce statistics. */
+int pf_check_state(pf_ctx *ctx, const double reference_totals[2], double max_rel_drift, double out[8]);
 int pf_synchronize(pf_ctx *ctx);
 int pf_get_time(pf_ctx *ctx, double *time);
 int pf_last_params(pf_ctx *ctx, pf_step_params *out);

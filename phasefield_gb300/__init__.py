@@ -129,6 +129,7 @@ SYMBOLS = {
     "pf_diffuse": (_I, [_P, _I]),
     "pf_reduce": (_I, [_P, _DP]),
     "pf_synchronize": (_I, [_P]),
+    "pf_check_state": (_I, [_P, _DP, _D, _DP]),
     "pf_get_time": (_I, [_P, _DP]),
     "pf_last_params": (_I, [_P, ctypes.POINTER(PfStepParams)]),
     "pf_truncated_cells": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
@@ -292,6 +293,11 @@ class PhaseField:
         out = np.zeros(8, np.float64)
         check(lib().pf_reduce(self._ctx, out.ctypes.data_as(_DP)), "pf_reduce")
         return out
+
+    def check_state(self, reference_totals=None, max_rel_drift: float = 0.0) -> int:
+        """Status of pf_check_state (PF_OK or PF_ERR_NONFINITE), without raising."""
+        ref = None if reference_totals is None else np.ascontiguousarray(reference_totals, np.float64)
+        return lib().pf_check_state(self._ctx, None if ref is None else ref.ctypes.data_as(_DP), max_rel_drift, None)
 
     def fractions(self) -> np.ndarray:
         """write_data.cpp:14-18: phase volume fractions and the deformed fraction."""

@@ -657,6 +657,22 @@ extern "C" int pf_reduce(pf_ctx *c, double out[8]) {
     return PF_OK;
 }
 
+extern "C" int pf_check_state(pf_ctx *c, const double reference_totals[2], double max_rel_drift, double out[8]) {
+    double r[8];
+    int st = pf_reduce(c, r);
+    if (st != PF_OK) return st;
+    if (out)
+        for (int i = 0; i < 8; i++) out[i] = r[i];
+    if (r[7] > 0) return pf_fail(PF_ERR_NONFINITE, "pf_check_state: non-finite values in the state");
+    if (reference_totals && max_rel_drift > 0)
+        for (int q = 0; q < c->nsol; q++) {
+            const double ref = reference_totals[q];
+            if (ref != 0.0 && std::abs(r[4 + q] - ref) > max_rel_drift * std::abs(ref))
+                return pf_fail(PF_ERR_NONFINITE, "pf_check_state: solute total drifted beyond the tolerance");
+        }
+    return PF_OK;
+}
+
 extern "C" int pf_synchronize(pf_ctx *c) {
     if (!c) return pf_fail(PF_ERR_ARG, "pf_synchronize: null context");
     PF_CUDA_OK(cudaStreamSynchronize(c->stream));
