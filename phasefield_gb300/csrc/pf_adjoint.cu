@@ -218,8 +218,10 @@ __global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R
     for (int p = 0; p < 3; p++) {
         const R c0 = dc[p * P.N + n];
         R a = 0;
-        for (int b = 0; b < P.nnb; b++) a += ds[p * P.N + nb[b]] * (dc[p * P.N + nb[b]] - c0);
-        f += ds[p * P.N + n] * P.D[p] * a;
+        // The diffusion sums carry no discrete decision: fused multiply-adds
+        // are used explicitly (this file is otherwise built without contraction).
+        for (int b = 0; b < P.nnb; b++) a = fma(ds[p * P.N + nb[b]], dc[p * P.N + nb[b]] - c0, a);
+        f = fma(ds[p * P.N + n] * P.D[p], a, f);
     }
     C2[n] = C[n] + f;
 }
@@ -244,14 +246,14 @@ __global__ void k_bwd_diffuse_d(const AP<R> P, const R *ph, const R *ds, const R
             for (int b = 0; b < P.nnb; b++) {
                 const long long m = nb[b];
                 const R sm = ds[p * P.N + m], dcm = dc[p * P.N + m] - c0, lm = lam[m];
-                al += sm * (lm - l0);
-                ac += sm * dcm;
-                ads += sm * dcm * (l0 - lm);
+                al = fma(sm, lm - l0, al);
+                ac = fma(sm, dcm, ac);
+                ads = fma(sm * dcm, l0 - lm, ads);
             }
-            out += P.D[p] * s0 * dit[p * P.N + n] * al;
+            out = fma(P.D[p] * s0 * dit[p * P.N + n], al, out);
             dL_dc[p] = P.D[p] * s0 * al;
             dL_ds[p] = P.D[p] * ads;
-            flux += s0 * P.D[p] * ac;
+            flux = fma(s0 * P.D[p], ac, flux);
         }
         lam2[n] = out;
         for (int j = 0; j < 3; j++) {
@@ -333,7 +335,7 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
     if (n < P.N) {
         Lst<R> L;
         build_list(P, n, gid, phi, C, L);
-        for (int e = 0; e < LMAX; e++) pub_id[LMAX * n + e] = 0;
+        pub_id[LMAX * n] = 0;  // empty published list unless the cell is an interface cell
         if (L.bulk) {
             for (int a = 0; a < 4; a++) lphi_pre[4 * n + a] = lphi_post[4 * n + a];
             for (int p = 0; p < 3; p++) lph_pre[3 * n + p] = lph_post[3 * n + p];
@@ -412,6 +414,7 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
                 pub_id[LMAX * n + e] = L.id[e];
                 pub_l[LMAX * n + e] = lS[e];
             }
+            if (L.num < LMAX) pub_id[LMAX * n + L.num] = 0;  // terminator (the gather stops at id 0)
         }
     }
     for (int s = 16; s > 0; s >>= 1) {
