@@ -230,7 +230,9 @@ def run_adjoint(args) -> dict:
     st = pf.init_microstructure(m, wl.spec(), 0.0)
     A = pf.Adjoint(m, pf.PF_PREC_FP32C, 100)
     A.upload(st, 0.0)
-    A.forward(min(args.adjoint_steps, 100))  # warm-up
+    # Warm-up: builds the forward graph and the segment graph (both reused below).
+    A.forward(min(args.adjoint_steps, 200))
+    A.gradient(0)
     J = A.forward(args.adjoint_steps)
     g = A.gradient(0)
     t = A.timings()

@@ -502,8 +502,9 @@ struct AdjCtx : pf_adj_impl {
     // segment storage: per step pre-step state and pre-sub-step carbon
     std::vector<ushort4 *> sg_gid;
     std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;
-    ushort4 *w_gid = nullptr;
+    ushort4 *w_gid = nullptr, *v_gid = nullptr;  // w_*, v_*: the forward's two state sets
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
+    R *v_phi = nullptr, *v_ph = nullptr, *v_C = nullptr;
     R *d_s = nullptr, *d_c = nullptr, *d_it = nullptr;  // derived planes of one sub-step
     // adjoint buffers
     R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
@@ -518,6 +519,7 @@ struct AdjCtx : pf_adj_impl {
     // and recompute + reverse sweep.  Rebuilt whenever the parameters change.
     cudaGraphExec_t fwd_graph[2] = {nullptr, nullptr};
     cudaGraphExec_t seg_graph = nullptr;
+    AP<R> gP{};  // parameters the graphs were captured with
     R *g_C = nullptr, *g_phi = nullptr, *g_ph = nullptr;  // adjoint buffer roles at capture
     const R *fin_ph = nullptr, *fin_C = nullptr;            // final state of the last forward run
 
@@ -535,6 +537,7 @@ struct AdjCtx : pf_adj_impl {
         for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
         for (size_t i = 0; i < sg_gid.size(); i++) { f(sg_gid[i]); f(sg_phi[i]); f(sg_ph[i]); f(sg_C[i]); f(sg_Csub[i]); }
         f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(d_s); f(d_c); f(d_it);
+        f(v_gid); f(v_phi); f(v_ph); f(v_C);
         f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
         if (s) cudaStreamDestroy(s);
     }
@@ -608,6 +611,7 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
     ok = ok && c->alloc(&c->d_s, 3 * N) && c->alloc(&c->d_c, 3 * N) && c->alloc(&c->d_it, 3 * N);
+    ok = ok && c->alloc(&c->v_gid, N) && c->alloc(&c->v_phi, 4 * N) && c->alloc(&c->v_ph, 3 * N) && c->alloc(&c->v_C, N);
     ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
          c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
     ok = ok && c->alloc(&c->l_phi, 4 * N) && c->alloc(&c->l_ph, 3 * N) && c->alloc(&c->l_C, N) &&
@@ -753,11 +757,15 @@ static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
     cudaEventRecord(e0, c->s);
     // Two state sets alternate: the work buffers and the spare checkpoint slot
     // (slot nck-1 is never a checkpoint).  Checkpoints are copies taken every K steps.
-    ushort4 *ga = c->w_gid, *gb = c->ck_gid[nck - 1];
-    R *pa = c->w_phi, *pb = c->ck_phi[nck - 1], *ha = c->w_ph, *hb = c->ck_ph[nck - 1];
-    R *Ca = c->w_C, *Cb = c->ck_C[nck - 1];
+    ushort4 *ga = c->w_gid, *gb = c->v_gid;
+    R *pa = c->w_phi, *pb = c->v_phi, *ha = c->w_ph, *hb = c->v_ph;
+    R *Ca = c->w_C, *Cb = c->v_C;
     copy_state(c, c->gid0, c->phi0, c->ph0, c->C0, ga, pa, ha, Ca);
-    c->drop_graphs();
+    // Captured graphs bake the parameters in: keep them while they are unchanged.
+    if (std::memcmp(&c->gP, &c->P, sizeof(c->P)) != 0) {
+        c->drop_graphs();
+        c->gP = c->P;
+    }
     // A full segment of K steps is one CUDA graph (per starting buffer set);
     // the checkpoint copy in front of it depends on the segment and stays outside.
     auto run_steps = [&](int n) -> int {
