@@ -160,9 +160,24 @@ __device__ void build_list(const AP<R> &P, long long n, const ushort4 *gid, cons
 }
 
 // ---------------------------------------------------------------- forward --
+// Derived planes of one cell for one sub-step: s_p = sqrt(phi_p), c_p
+// (partitioned carbon) and 1/t1_p, each stored as three planes.
+template <typename R>
+__device__ __forceinline__ void derive_cell(const AP<R> &P, long long n, const R p[3], R C, R *ds, R *dc, R *dit) {
+    R c[3], t[3];
+    partition(P, C, p, c, t);
+    for (int q = 0; q < 3; q++) {
+        ds[q * P.N + n] = sqrt(p[q]);
+        dc[q * P.N + n] = c[q];
+        dit[q * P.N + n] = (R)1 / t[q];
+    }
+}
+
+// Phase sweep; also writes the derived planes of the first diffusion sub-step
+// (the new phase fractions with the unchanged carbon).
 template <typename R>
 __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
-                            R *phi2, R *ph2) {
+                            R *phi2, R *ph2, R *ds, R *dc, R *dit) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= P.N) return;
     Lst<R> L;
@@ -170,7 +185,9 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
     if (L.bulk) {
         gid2[n] = gid[n];
         for (int a = 0; a < 4; a++) phi2[4 * n + a] = phi[4 * n + a];
-        for (int p = 0; p < 3; p++) ph2[3 * n + p] = ph[3 * n + p];
+        const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+        for (int p = 0; p < 3; p++) ph2[3 * n + p] = pp[p];
+        derive_cell(P, n, pp, C[n], ds, dc, dit);
         return;
     }
     const R inv = (R)1 / L.sum;
@@ -187,29 +204,20 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
         phi2[4 * n + a] = v;
     }
     gid2[n] = make_ushort4((unsigned short)oid[0], (unsigned short)oid[1], (unsigned short)oid[2], (unsigned short)oid[3]);
-    for (int p = 0; p < 3; p++) ph2[3 * n + p] = q[p] * inv;
-}
-
-// Per-cell derived quantities of one sub-step, formed once: s_p = sqrt(phi_p),
-// c_p (partitioned carbon) and 1/t1_p, each as three planes.
-template <typename R>
-__global__ void k_derive(const AP<R> P, const R *ph, const R *C, R *ds, R *dc, R *dit) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
-    const R p[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
-    R c[3], t[3];
-    partition(P, C[n], p, c, t);
-    for (int q = 0; q < 3; q++) {
-        ds[q * P.N + n] = sqrt(p[q]);
-        dc[q * P.N + n] = c[q];
-        dit[q * P.N + n] = (R)1 / t[q];
+    R pp[3];
+    for (int p = 0; p < 3; p++) {
+        pp[p] = q[p] * inv;
+        ph2[3 * n + p] = pp[p];
     }
+    derive_cell(P, n, pp, C[n], ds, dc, dit);
 }
 
 // Forward sub-step (solver.cpp:343-372) from the derived planes:
-//   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p).
+//   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p);
+// with ds2 != NULL it also writes the next sub-step's derived planes.
 template <typename R>
-__global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2) {
+__global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2, const R *ph, R *ds2,
+                                R *dc2, R *dit2) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= P.N) return;
     long long nb[6];
@@ -223,7 +231,12 @@ __global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R
         for (int b = 0; b < P.nnb; b++) a = fma(ds[p * P.N + nb[b]], dc[p * P.N + nb[b]] - c0, a);
         f = fma(ds[p * P.N + n] * P.D[p], a, f);
     }
-    C2[n] = C[n] + f;
+    const R cn = C[n] + f;
+    C2[n] = cn;
+    if (ds2) {
+        const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
+        derive_cell(P, n, pp, cn, ds2, dc2, dit2);
+    }
 }
 
 // Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
@@ -505,7 +518,7 @@ struct AdjCtx : pf_adj_impl {
     ushort4 *w_gid = nullptr, *v_gid = nullptr;  // w_*, v_*: the forward's two state sets
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
     R *v_phi = nullptr, *v_ph = nullptr, *v_C = nullptr;
-    R *d_s = nullptr, *d_c = nullptr, *d_it = nullptr;  // derived planes of one sub-step
+    R *dscr = nullptr;  // two scratch slots of derived planes (9N each)
     // adjoint buffers
     R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
     int *pub_id = nullptr;
@@ -536,7 +549,7 @@ struct AdjCtx : pf_adj_impl {
         f(gid0); f(phi0); f(ph0); f(C0);
         for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
         for (size_t i = 0; i < sg_gid.size(); i++) { f(sg_gid[i]); f(sg_phi[i]); f(sg_ph[i]); f(sg_C[i]); f(sg_Csub[i]); }
-        f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(d_s); f(d_c); f(d_it);
+        f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(dscr);
         f(v_gid); f(v_phi); f(v_ph); f(v_C);
         f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
         if (s) cudaStreamDestroy(s);
@@ -575,18 +588,21 @@ struct AdjCtx : pf_adj_impl {
     int step(const ushort4 *g, const R *phi, const R *ph, const R *C, ushort4 *g2, R *phi2, R *ph2, R *C2,
              R *Dsub) {
         const unsigned nb = blocks(N);
-        k_fwd_phase<R><<<nb, 256, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2);
+        // Derived planes of sub-step k: slot k of Dsub, or one of two scratch
+        // slots used alternately.
+        auto slot = [&](int k) -> R * { return Dsub ? Dsub + (size_t)k * 9 * N : dscr + (size_t)(k & 1) * 9 * N; };
+        R *d0 = slot(0);
+        k_fwd_phase<R><<<nb, 256, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0, d0 + 3 * N, d0 + 6 * N);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
         // one lands in C2 and no sub-step reads the buffer it writes.
         R *buf[2] = {C2, w_C2};
         const R *cin = C;
         for (int k = 0; k < n_sub; k++) {
             R *cout = buf[(n_sub - 1 - k) % 2];
-            R *ds = Dsub ? Dsub + (size_t)k * 9 * N : d_s;
-            R *dc = Dsub ? ds + 3 * N : d_c;
-            R *dit = Dsub ? ds + 6 * N : d_it;
-            k_derive<R><<<nb, 256, 0, s>>>(P, ph2, cin, ds, dc, dit);
-            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, ds, dc, cin, cout);
+            R *dk = slot(k);
+            R *dn = (k + 1 < n_sub) ? slot(k + 1) : nullptr;
+            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, dk, dk + 3 * N, cin, cout, ph2, dn, dn ? dn + 3 * N : nullptr,
+                                                  dn ? dn + 6 * N : nullptr);
             cin = cout;
         }
         return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
@@ -610,7 +626,7 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     const size_t N = (size_t)c->N;
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
-    ok = ok && c->alloc(&c->d_s, 3 * N) && c->alloc(&c->d_c, 3 * N) && c->alloc(&c->d_it, 3 * N);
+    ok = ok && c->alloc(&c->dscr, 18 * N);
     ok = ok && c->alloc(&c->v_gid, N) && c->alloc(&c->v_phi, 4 * N) && c->alloc(&c->v_ph, 3 * N) && c->alloc(&c->v_C, N);
     ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
          c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
