@@ -56,7 +56,6 @@ struct AP {
 
 __device__ __forceinline__ int lphase(int l, int b1, int b2) { return l == 0 ? 0 : (l <= b1 ? 1 : (l <= b2 ? 2 : 3)); }
 
-__device__ __forceinline__ void neighbours(long long n, int ix, int iy, int iz, long long nb[6]) { pf_neighbours(n, ix, iy, iz, nb); }
 
 template <typename R>
 __device__ __forceinline__ void partition(const AP<R> &P, R C, const R ph[3], R c[3], R t1[3]) {
@@ -85,9 +84,10 @@ struct Lst {
 };
 
 template <typename R>
-__device__ void build_list(const AP<R> &P, long long n, const ushort4 *gid, const R *phi, const R *C, Lst<R> &L) {
+__device__ void build_list(const AP<R> &P, int ci, int cj, int ck, long long n, const ushort4 *gid, const R *phi,
+                           const R *C, Lst<R> &L) {
     long long nb[6];
-    neighbours(n, P.ix, P.iy, P.iz, nb);
+    pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
     const ushort4 g = gid[n];
     L.oid[0] = g.x; L.oid[1] = g.y; L.oid[2] = g.z; L.oid[3] = g.w;
     for (int a = 0; a < 4; a++) L.ov[a] = phi[4 * n + a];
@@ -178,10 +178,11 @@ __device__ __forceinline__ void derive_cell(const AP<R> &P, long long n, const R
 template <typename R>
 __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
                             R *phi2, R *ph2, R *ds, R *dc, R *dit) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     Lst<R> L;
-    build_list(P, n, gid, phi, C, L);
+    build_list(P, ci, cj, ck, n, gid, phi, C, L);
     if (L.bulk) {
         gid2[n] = gid[n];
         for (int a = 0; a < 4; a++) phi2[4 * n + a] = phi[4 * n + a];
@@ -218,10 +219,11 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
 template <typename R>
 __global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2, const R *ph, R *ds2,
                                 R *dc2, R *dit2) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nb[6];
-    neighbours(n, P.ix, P.iy, P.iz, nb);
+    pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
     R f = 0;
     for (int p = 0; p < 3; p++) {
         const R c0 = dc[p * P.N + n];
@@ -246,11 +248,13 @@ __global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R
 template <typename R>
 __global__ void k_bwd_diffuse_d(const AP<R> P, const R *ph, const R *ds, const R *dc, const R *dit, const R *lam,
                                 R *lam2, R *lph, double *grad) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int ci, cj, ck;
+    long long n;
+    const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
     double g = 0;
-    if (n < P.N) {
+    if (in) {
         long long nb[6];
-        neighbours(n, P.ix, P.iy, P.iz, nb);
+        pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
         const R l0 = lam[n];
         R out = l0, dL_ds[3], dL_dc[3], flux = 0;
         for (int p = 0; p < 3; p++) {
@@ -343,11 +347,13 @@ template <typename R>
 __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph_pre, const R *C,
                                 const R *lphi_post, const R *lph_post, R *lC, R *lphi_pre, R *lph_pre, int *pub_id,
                                 R *pub_l, double *grad) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int ci, cj, ck;
+    long long n;
+    const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
     double gm = 0, gs = 0;
-    if (n < P.N) {
+    if (in) {
         Lst<R> L;
-        build_list(P, n, gid, phi, C, L);
+        build_list(P, ci, cj, ck, n, gid, phi, C, L);
         pub_id[LMAX * n] = 0;  // empty published list unless the cell is an interface cell
         if (L.bulk) {
             for (int a = 0; a < 4; a++) lphi_pre[4 * n + a] = lphi_post[4 * n + a];
@@ -445,10 +451,11 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
 // published adjoint of their stencil sum for that grain.
 template <typename R>
 __global__ void k_bwd_phase_gather(const AP<R> P, const ushort4 *gid, const int *pub_id, const R *pub_l, R *lphi_pre) {
-    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= P.N) return;
+    int ci, cj, ck;
+    long long m;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, m)) return;
     long long nb[6];
-    neighbours(m, P.ix, P.iy, P.iz, nb);
+    pf_neighbours3(ci, cj, ck, m, P.ix, P.iy, P.iz, nb);
     const ushort4 g = gid[m];
     const int id[4] = {g.x, g.y, g.z, g.w};
     R add[4] = {0, 0, 0, 0};
@@ -587,12 +594,12 @@ struct AdjCtx : pf_adj_impl {
     // every sub-step (s_p, c_p, 1/t1_p) are kept there for the reverse sweep.
     int step(const ushort4 *g, const R *phi, const R *ph, const R *C, ushort4 *g2, R *phi2, R *ph2, R *C2,
              R *Dsub) {
-        const unsigned nb = blocks(N);
+        const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
         // Derived planes of sub-step k: slot k of Dsub, or one of two scratch
         // slots used alternately.
         auto slot = [&](int k) -> R * { return Dsub ? Dsub + (size_t)k * 9 * N : dscr + (size_t)(k & 1) * 9 * N; };
         R *d0 = slot(0);
-        k_fwd_phase<R><<<nb, 256, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0, d0 + 3 * N, d0 + 6 * N);
+        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0, d0 + 3 * N, d0 + 6 * N);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
         // one lands in C2 and no sub-step reads the buffer it writes.
         R *buf[2] = {C2, w_C2};
@@ -601,7 +608,7 @@ struct AdjCtx : pf_adj_impl {
             R *cout = buf[(n_sub - 1 - k) % 2];
             R *dk = slot(k);
             R *dn = (k + 1 < n_sub) ? slot(k + 1) : nullptr;
-            k_fwd_diffuse_d<R><<<nb, 256, 0, s>>>(P, dk, dk + 3 * N, cin, cout, ph2, dn, dn ? dn + 3 * N : nullptr,
+            k_fwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, dk, dk + 3 * N, cin, cout, ph2, dn, dn ? dn + 3 * N : nullptr,
                                                   dn ? dn + 6 * N : nullptr);
             cin = cout;
         }
@@ -855,6 +862,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     const size_t N = (size_t)c->N;
     const unsigned nb = blocks(c->N);
     AP<R> P = c->P;
+    const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, c->s);
@@ -885,14 +893,14 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
             // Reverse the diffusion sub-steps.
             for (int k = c->n_sub - 1; k >= 0; k--) {
                 const R *ds = c->sg_Csub[i] + (size_t)k * 9 * N;
-                k_bwd_diffuse_d<R><<<nb, 256, 0, c->s>>>(P, ph_post, ds, ds + 3 * N, ds + 6 * N, c->l_C, c->l_C2, c->l_ph,
+                k_bwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, ph_post, ds, ds + 3 * N, ds + 6 * N, c->l_C, c->l_C2, c->l_ph,
                                                         c->d_acc + 3);
                 std::swap(c->l_C, c->l_C2);
             }
             // Reverse the phase sweep.
-            k_bwd_phase_own<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
+            k_bwd_phase_own<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
                                                     c->l_ph, c->l_C, c->l_phi2, c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
-            k_bwd_phase_gather<R><<<nb, 256, 0, c->s>>>(P, c->sg_gid[i], c->pub_id, c->pub_l, c->l_phi2);
+            k_bwd_phase_gather<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->sg_gid[i], c->pub_id, c->pub_l, c->l_phi2);
             std::swap(c->l_phi, c->l_phi2);
             std::swap(c->l_ph, c->l_ph2);
         }

@@ -35,6 +35,35 @@ __device__ __forceinline__ void pf_neighbours(long long n, int ix, int iy, int i
     nbr[5] = i + (long long)ix * j + plane * pf_wrap(k, iz, 1);
 }
 
+// One-thread-per-cell kernels run on a (ceil(ix/256), iy, iz) grid of 256-thread
+// blocks: the cell's coordinates come from the block coordinates (no integer
+// division), and a thread with i >= ix has no cell.
+constexpr int PF_CELL_THREADS = 256;
+
+inline dim3 pf_cell_grid(int ix, int iy, int iz) {
+    return dim3((unsigned)((ix + PF_CELL_THREADS - 1) / PF_CELL_THREADS), (unsigned)iy, (unsigned)iz);
+}
+
+__device__ __forceinline__ bool pf_cell(int ix, int iy, int &i, int &j, int &k, long long &n) {
+    i = blockIdx.x * PF_CELL_THREADS + threadIdx.x;
+    j = blockIdx.y;
+    k = blockIdx.z;
+    n = i + (long long)ix * (j + (long long)iy * k);
+    return i < ix;
+}
+
+// Neighbours of (i,j,k) in the reference order x-, x+, y-, y+, z-, z+.
+__device__ __forceinline__ void pf_neighbours3(int i, int j, int k, long long n, int ix, int iy, int iz,
+                                               long long nbr[6]) {
+    const long long plane = (long long)ix * iy;
+    nbr[0] = n - i + pf_wrap(i, ix, -1);
+    nbr[1] = n - i + pf_wrap(i, ix, 1);
+    nbr[2] = n + (long long)ix * (pf_wrap(j, iy, -1) - j);
+    nbr[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
+    nbr[4] = n + plane * (pf_wrap(k, iz, -1) - k);
+    nbr[5] = n + plane * (pf_wrap(k, iz, 1) - k);
+}
+
 #define PF_CUDA_OK(call)                                  \
     do {                                                  \
         cudaError_t e_ = (call);                          \

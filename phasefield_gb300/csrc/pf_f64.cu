@@ -49,10 +49,11 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                                                    double *__restrict__ phase,
                                                    double *__restrict__ conc1,
                                                    const double *__restrict__ C) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nbr[6];
-    pf_neighbours(n, P.ix, P.iy, P.iz, nbr);
+    pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nbr);
     const double cutoff = P.cutoff;
 
     // 1-based stencil arrays of the reference become 0-based position arrays.
@@ -260,10 +261,11 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
                                                      const double *__restrict__ conc1,
                                                      double *__restrict__ conc2,
                                                      double *__restrict__ C) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.N) return;
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nbr[6];
-    pf_neighbours(n, P.ix, P.iy, P.iz, nbr);
+    pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nbr);
     double ph[3];
     ph[0] = __ldg(phase + 3 * n + 0);
     ph[1] = __ldg(phase + 3 * n + 1);
@@ -323,13 +325,13 @@ inline unsigned pf_blocks(long long N, int threads) { return (unsigned)((N + thr
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
                                 double *phi2, double *phase, double *conc1, const double *C,
                                 cudaStream_t s) {
-    k_phase_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C);
+    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C);
     return cudaGetLastError();
 }
 
 cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
                                   const double *conc1, double *conc2, double *C, cudaStream_t s) {
-    k_diffuse_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, nnb, coef, phase, conc1, conc2, C);
+    k_diffuse_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, coef, phase, conc1, conc2, C);
     return cudaGetLastError();
 }
 
