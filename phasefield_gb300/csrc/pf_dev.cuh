@@ -19,22 +19,6 @@ __device__ __forceinline__ int pf_phase_of_grain(int g) {
     return q > 0 ? q : 1;
 }
 
-// Neighbour linear indices in the reference order x-, x+, y-, y+, z-, z+
-// (solver.cpp:159-166, :353-358).
-__device__ __forceinline__ void pf_neighbours(long long n, int ix, int iy, int iz, long long nbr[6]) {
-    const int i = (int)(n % ix);
-    const long long r = n / ix;
-    const int j = (int)(r % iy);
-    const int k = (int)(r / iy);
-    const long long plane = (long long)ix * iy;
-    nbr[0] = pf_wrap(i, ix, -1) + (long long)ix * j + plane * k;
-    nbr[1] = pf_wrap(i, ix, 1) + (long long)ix * j + plane * k;
-    nbr[2] = i + (long long)ix * pf_wrap(j, iy, -1) + plane * k;
-    nbr[3] = i + (long long)ix * pf_wrap(j, iy, 1) + plane * k;
-    nbr[4] = i + (long long)ix * j + plane * pf_wrap(k, iz, -1);
-    nbr[5] = i + (long long)ix * j + plane * pf_wrap(k, iz, 1);
-}
-
 // One-thread-per-cell kernels run on a (ceil(ix/256), iy, iz) grid of 256-thread
 // blocks: the cell's coordinates come from the block coordinates (no integer
 // division), and a thread with i >= ix has no cell.
@@ -52,7 +36,8 @@ __device__ __forceinline__ bool pf_cell(int ix, int iy, int &i, int &j, int &k, 
     return i < ix;
 }
 
-// Neighbours of (i,j,k) in the reference order x-, x+, y-, y+, z-, z+.
+// Neighbours of (i,j,k) in the reference order x-, x+, y-, y+, z-, z+
+// (solver.cpp:159-166, :353-358).
 __device__ __forceinline__ void pf_neighbours3(int i, int j, int k, long long n, int ix, int iy, int iz,
                                                long long nbr[6]) {
     const long long plane = (long long)ix * iy;
