@@ -160,40 +160,24 @@ __device__ void build_list(const AP<R> &P, int ci, int cj, int ck, long long n, 
 }
 
 // ---------------------------------------------------------------- forward --
-// Derived record of one cell for one sub-step, stored contiguously
-// (REC values per cell, 16-byte aligned): s_p = sqrt(phi_p) at [0..2], the
-// partitioned carbon c_p at [3..5] and 1/t1_p at [6..8].
-constexpr int REC = 12;
-
+// Derived planes of one cell for one sub-step: s_p = sqrt(phi_p), c_p
+// (partitioned carbon) and 1/t1_p, each stored as three planes.
 template <typename R>
-__device__ __forceinline__ void derive_cell(const AP<R> &P, long long n, const R p[3], R C, R *rec) {
+__device__ __forceinline__ void derive_cell(const AP<R> &P, long long n, const R p[3], R C, R *ds, R *dc, R *dit) {
     R c[3], t[3];
     partition(P, C, p, c, t);
-    R *r = rec + (long long)REC * n;
     for (int q = 0; q < 3; q++) {
-        r[q] = sqrt(p[q]);
-        r[3 + q] = c[q];
-        r[6 + q] = (R)1 / t[q];
+        ds[q * P.N + n] = sqrt(p[q]);
+        dc[q * P.N + n] = c[q];
+        dit[q * P.N + n] = (R)1 / t[q];
     }
 }
 
-// The six values s_p, c_p of a cell (two or three vector loads).
-__device__ __forceinline__ void load_sc(const float *rec, long long n, float sc[6]) {
-    const float4 a = reinterpret_cast<const float4 *>(rec + REC * n)[0];
-    const float2 b = reinterpret_cast<const float2 *>(rec + REC * n)[2];
-    sc[0] = a.x; sc[1] = a.y; sc[2] = a.z; sc[3] = a.w; sc[4] = b.x; sc[5] = b.y;
-}
-__device__ __forceinline__ void load_sc(const double *rec, long long n, double sc[6]) {
-    const double2 *v = reinterpret_cast<const double2 *>(rec + REC * n);
-    const double2 a = v[0], b = v[1], c = v[2];
-    sc[0] = a.x; sc[1] = a.y; sc[2] = b.x; sc[3] = b.y; sc[4] = c.x; sc[5] = c.y;
-}
-
-// Phase sweep; also writes the derived records of the first diffusion sub-step
+// Phase sweep; also writes the derived planes of the first diffusion sub-step
 // (the new phase fractions with the unchanged carbon).
 template <typename R>
 __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
-                            R *phi2, R *ph2, R *rec) {
+                            R *phi2, R *ph2, R *ds, R *dc, R *dit) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
@@ -204,7 +188,7 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
         for (int a = 0; a < 4; a++) phi2[4 * n + a] = phi[4 * n + a];
         const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
         for (int p = 0; p < 3; p++) ph2[3 * n + p] = pp[p];
-        derive_cell(P, n, pp, C[n], rec);
+        derive_cell(P, n, pp, C[n], ds, dc, dit);
         return;
     }
     const R inv = (R)1 / L.sum;
@@ -226,45 +210,44 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
         pp[p] = q[p] * inv;
         ph2[3 * n + p] = pp[p];
     }
-    derive_cell(P, n, pp, C[n], rec);
+    derive_cell(P, n, pp, C[n], ds, dc, dit);
 }
 
-// Forward sub-step (solver.cpp:343-372) from the derived records:
+// Forward sub-step (solver.cpp:343-372) from the derived planes:
 //   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p);
-// with rec2 != NULL it also writes the next sub-step's records.
+// with ds2 != NULL it also writes the next sub-step's derived planes.
 template <typename R>
-__global__ void k_fwd_diffuse_d(const AP<R> P, const R *rec, const R *C, R *C2, const R *ph, R *rec2) {
+__global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2, const R *ph, R *ds2,
+                                R *dc2, R *dit2) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nb[6];
     pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
-    R own[6];
-    load_sc(rec, n, own);
-    R a[3] = {0, 0, 0};
-    // The diffusion sums carry no discrete decision: fused multiply-adds are
-    // used explicitly (this file is otherwise built without contraction).
-    for (int b = 0; b < P.nnb; b++) {
-        R m[6];
-        load_sc(rec, nb[b], m);
-        for (int p = 0; p < 3; p++) a[p] = fma(m[p], m[3 + p] - own[3 + p], a[p]);
-    }
     R f = 0;
-    for (int p = 0; p < 3; p++) f = fma(own[p] * P.D[p], a[p], f);
+    for (int p = 0; p < 3; p++) {
+        const R c0 = dc[p * P.N + n];
+        R a = 0;
+        // The diffusion sums carry no discrete decision: fused multiply-adds
+        // are used explicitly (this file is otherwise built without contraction).
+        for (int b = 0; b < P.nnb; b++) a = fma(ds[p * P.N + nb[b]], dc[p * P.N + nb[b]] - c0, a);
+        f = fma(ds[p * P.N + n] * P.D[p], a, f);
+    }
     const R cn = C[n] + f;
     C2[n] = cn;
-    if (rec2) {
+    if (ds2) {
         const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
-        derive_cell(P, n, pp, cn, rec2);
+        derive_cell(P, n, pp, cn, ds2, dc2, dit2);
     }
 }
 
 // Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
-// sub-step), the derived records of the state before it.  Out: lam2 (adjoint
-// of C before), lph += the phase-fraction part (through s_p and c_p(phi)),
-// grad[2] += dJ/ds_C.
+// sub-step), the derived planes of the state before it, ph.  Out: lam2
+// (adjoint of C before), lph += the phase-fraction part (through s_p and
+// c_p(phi)), grad[2] += dJ/ds_C.
 template <typename R>
-__global__ void k_bwd_diffuse_d(const AP<R> P, const R *rec, const R *lam, R *lam2, R *lph, double *grad) {
+__global__ void k_bwd_diffuse_d(const AP<R> P, const R *ph, const R *ds, const R *dc, const R *dit, const R *lam,
+                                R *lam2, R *lph, double *grad) {
     int ci, cj, ck;
     long long n;
     const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
@@ -272,36 +255,30 @@ __global__ void k_bwd_diffuse_d(const AP<R> P, const R *rec, const R *lam, R *la
     if (in) {
         long long nb[6];
         pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
-        R own[6];
-        load_sc(rec, n, own);
         const R l0 = lam[n];
-        R al[3] = {0, 0, 0}, ac[3] = {0, 0, 0}, ads[3] = {0, 0, 0};
-        for (int b = 0; b < P.nnb; b++) {
-            R m[6];
-            load_sc(rec, nb[b], m);
-            const R lm = lam[nb[b]];
-            for (int p = 0; p < 3; p++) {
-                const R dcm = m[3 + p] - own[3 + p];
-                al[p] = fma(m[p], lm - l0, al[p]);
-                ac[p] = fma(m[p], dcm, ac[p]);
-                ads[p] = fma(m[p] * dcm, l0 - lm, ads[p]);
-            }
-        }
-        const R *r = rec + (long long)REC * n;
-        const R it[3] = {r[6], r[7], r[8]};
         R out = l0, dL_ds[3], dL_dc[3], flux = 0;
         for (int p = 0; p < 3; p++) {
-            const R s0 = own[p];
-            out = fma(P.D[p] * s0 * it[p], al[p], out);
-            dL_dc[p] = P.D[p] * s0 * al[p];
-            dL_ds[p] = P.D[p] * ads[p];
-            flux = fma(s0 * P.D[p], ac[p], flux);
+            const R s0 = ds[p * P.N + n], c0 = dc[p * P.N + n];
+            R al = 0, ac = 0, ads = 0;
+            for (int b = 0; b < P.nnb; b++) {
+                const long long m = nb[b];
+                const R sm = ds[p * P.N + m], dcm = dc[p * P.N + m] - c0, lm = lam[m];
+                al = fma(sm, lm - l0, al);
+                ac = fma(sm, dcm, ac);
+                ads = fma(sm * dcm, l0 - lm, ads);
+            }
+            out = fma(P.D[p] * s0 * dit[p * P.N + n], al, out);
+            dL_dc[p] = P.D[p] * s0 * al;
+            dL_ds[p] = P.D[p] * ads;
+            flux = fma(s0 * P.D[p], ac, flux);
         }
         lam2[n] = out;
         for (int j = 0; j < 3; j++) {
             R v = 0;
-            for (int p = 0; p < 3; p++) v += dL_dc[p] * (-(P.c[p + 3 * j] + own[3 + p] * P.k[p + 3 * j]) * it[p]);
-            if (own[j] > (R)0) v += dL_ds[j] / ((R)2 * own[j]);
+            for (int p = 0; p < 3; p++)
+                v += dL_dc[p] * (-(P.c[p + 3 * j] + dc[p * P.N + n] * P.k[p + 3 * j]) * dit[p * P.N + n]);
+            const R sj = ds[j * P.N + n];
+            if (sj > (R)0) v += dL_ds[j] / ((R)2 * sj);
             lph[3 * n + j] += v;
         }
         g = (double)l0 * (double)flux / (double)P.s_c;
@@ -548,7 +525,7 @@ struct AdjCtx : pf_adj_impl {
     ushort4 *w_gid = nullptr, *v_gid = nullptr;  // w_*, v_*: the forward's two state sets
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
     R *v_phi = nullptr, *v_ph = nullptr, *v_C = nullptr;
-    R *dscr = nullptr;  // two scratch slots of derived records (REC*N each)
+    R *dscr = nullptr;  // two scratch slots of derived planes (9N each)
     // adjoint buffers
     R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
     int *pub_id = nullptr;
@@ -620,9 +597,9 @@ struct AdjCtx : pf_adj_impl {
         const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
         // Derived planes of sub-step k: slot k of Dsub, or one of two scratch
         // slots used alternately.
-        auto slot = [&](int k) -> R * { return Dsub ? Dsub + (size_t)k * REC * N : dscr + (size_t)(k & 1) * REC * N; };
+        auto slot = [&](int k) -> R * { return Dsub ? Dsub + (size_t)k * 9 * N : dscr + (size_t)(k & 1) * 9 * N; };
         R *d0 = slot(0);
-        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0);
+        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0, d0 + 3 * N, d0 + 6 * N);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
         // one lands in C2 and no sub-step reads the buffer it writes.
         R *buf[2] = {C2, w_C2};
@@ -631,7 +608,8 @@ struct AdjCtx : pf_adj_impl {
             R *cout = buf[(n_sub - 1 - k) % 2];
             R *dk = slot(k);
             R *dn = (k + 1 < n_sub) ? slot(k + 1) : nullptr;
-            k_fwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, dk, cin, cout, ph2, dn);
+            k_fwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, dk, dk + 3 * N, cin, cout, ph2, dn, dn ? dn + 3 * N : nullptr,
+                                                  dn ? dn + 6 * N : nullptr);
             cin = cout;
         }
         return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
@@ -655,7 +633,7 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     const size_t N = (size_t)c->N;
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
-    ok = ok && c->alloc(&c->dscr, 2 * REC * N);
+    ok = ok && c->alloc(&c->dscr, 18 * N);
     ok = ok && c->alloc(&c->v_gid, N) && c->alloc(&c->v_phi, 4 * N) && c->alloc(&c->v_ph, 3 * N) && c->alloc(&c->v_C, N);
     ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
          c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
@@ -770,7 +748,7 @@ static int ensure_ck(AdjCtx<R> *c, size_t nck, size_t nseg) {
     while (c->sg_gid.size() < nseg) {
         ushort4 *g; R *p, *h, *C, *Cs;
         if (!c->alloc(&g, N) || !c->alloc(&p, 4 * N) || !c->alloc(&h, 3 * N) || !c->alloc(&C, N) ||
-            !c->alloc(&Cs, (size_t)c->n_sub * REC * N)) {
+            !c->alloc(&Cs, (size_t)c->n_sub * 9 * N)) {
             cudaGetLastError();
             return pf_fail(PF_ERR_NOMEM, "adjoint segment allocation failed");
         }
@@ -908,11 +886,14 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     auto reverse = [&](int t0, int t1) {
         for (int t = t1 - 1; t >= t0; t--) {
             const int i = t - t0;
-            // Reverse the diffusion sub-steps (their derived records, taken
-            // from the post-sweep phase fractions, were kept by the recompute).
+            // Post-sweep phase fractions of step t: the diffusion leaves them
+            // alone, so they are the next step's stored pre-step values (or the
+            // segment's end state for its last step).
+            const R *ph_post = (t + 1 < t1) ? c->sg_ph[i + 1] : c->w_ph;
+            // Reverse the diffusion sub-steps.
             for (int k = c->n_sub - 1; k >= 0; k--) {
-                const R *rk = c->sg_Csub[i] + (size_t)k * REC * N;
-                k_bwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, rk, c->l_C, c->l_C2, c->l_ph,
+                const R *ds = c->sg_Csub[i] + (size_t)k * 9 * N;
+                k_bwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, ph_post, ds, ds + 3 * N, ds + 6 * N, c->l_C, c->l_C2, c->l_ph,
                                                         c->d_acc + 3);
                 std::swap(c->l_C, c->l_C2);
             }
