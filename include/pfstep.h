@@ -75,6 +75,7 @@ void GPU_Cleanup(void);
 #define PF_ERR_IO (-6)        /* file missing / malformed                    */
 #define PF_ERR_NODEV (-7)     /* no CUDA device                              */
 #define PF_ERR_RANGE (-8)     /* value outside what the layout can hold      */
+#define PF_ERR_DRIFT (-9)     /* a solute total drifted beyond the tolerance */
 
 #define PF_PREC_FP64 0   /* reference layout, FP64, bit-matching the CPU solver      */
 #define PF_PREC_FP32C 1  /* compact layout: 4 slots, uint16 ids, FP32 + Kahan solutes */
@@ -186,9 +187,10 @@ int pf_diffuse(pf_ctx *ctx, int nsub);
  * out[7] count of non-finite values.  Divide by N for write_data.cpp:14-18. */
 int pf_reduce(pf_ctx *ctx, double out[8]);
 /* Failure check on the FP64 statistics: PF_ERR_NONFINITE if any value of the
- * state is NaN/Inf, or if a solute total differs from reference_totals[q] by
- * more than max_rel_drift (relative; skipped when reference_totals is NULL or
- * max_rel_drift <= 0).  out (may be NULL) receives the pf_reduce statistics. */
+ * state is NaN/Inf; otherwise PF_ERR_DRIFT if a solute total differs from
+ * reference_totals[q] by more than max_rel_drift (relative; skipped when
+ * reference_totals is NULL or max_rel_drift <= 0).  out (may be NULL) receives
+ * the pf_reduce statistics. */
 int pf_check_state(pf_ctx *ctx, const double reference_totals[2], double max_rel_drift, double out[8]);
 int pf_synchronize(pf_ctx *ctx);
 int pf_get_time(pf_ctx *ctx, double *time);
@@ -203,11 +205,11 @@ int pf_kernel_times(pf_ctx *ctx, double times_ms[2], long long counts[2]);
 int pf_use_graph(pf_ctx *ctx, int on);
 /* Time every candidate tile shape of the FP32C diffusion kernel on the
  * context's own state and keep the fastest (state unchanged); reports the
- * chosen tile height, z chunk, kernel variant (0: two barriers per plane, 1:
- * double-buffered records) and mean launch time.  No-op for FP64. */
+ * chosen tile height, z chunk, kernel variant (always 0: one sub-step per
+ * pass over the grid) and mean launch time.  No-op for FP64. */
 int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *variant, float *ms);
-/* Fix the FP32C diffusion tile shape (tile_y 4/8/16, z chunk, variant 0/1);
- * tile_y = 0 returns to the default rule. */
+/* Fix the FP32C diffusion tile shape (tile_y 4/8/16, z chunk >= 1, variant
+ * 0; anything else is PF_ERR_ARG); tile_y = 0 returns to the default rule. */
 int pf_set_diffusion_tile(pf_ctx *ctx, int tile_y, int zchunk, int variant);
 /* The autotuner's candidates as (tile_y, zchunk, variant) triples; returns
  * how many were written (at most max). */
@@ -275,9 +277,11 @@ int pf_write_vti(const char *path, int ix, int iy, int iz, double dx, const int3
  * device synchronisation.  The scratch is a fixed 256 KiB __device__ array
  * held by every GPU that loads the library; N is limited to
  * PF_NOALLOC_MAX_CELLS (PF_ERR_RANGE beyond it).  The first call on a device
- * looks up the array's device address and should come before any stream
- * capture.  Asynchronous on cuda_stream (NULL = the legacy default stream);
- * calls that overlap on the GPU share the array and race. */
+ * looks up the array's device address (once per device, kept for the life of
+ * the process) and should come before any stream capture; a cudaDeviceReset
+ * invalidates that address, so calls on a device after it has been reset are
+ * not supported.  Asynchronous on cuda_stream (NULL = the legacy default
+ * stream); calls that overlap on the GPU share the array and race. */
 #define PF_NOALLOC_MAX_CELLS 16777216LL
 int pf_reduce_noalloc(long long N, int nsol, const int32_t *d_ids, const double *d_phi,
                       const double *d_phase, const double *d_C, double *d_out, void *cuda_stream);

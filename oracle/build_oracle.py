@@ -24,7 +24,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
-REF_SRC = "/root/reference/C++-openmp-cuda/src"
+# The zhubq/PhaseField checkout: PF_REFERENCE_ROOT, else a "reference" folder
+# beside the repository.  It is read only where it exists.
+REF_ROOT = os.path.abspath(os.environ.get("PF_REFERENCE_ROOT",
+                                          os.path.join(HERE, os.pardir, os.pardir, "reference")))
+REF_SRC = os.path.join(REF_ROOT, "C++-openmp-cuda", "src")
 REF_CUBIN = os.path.join(REF_OUT, "gpu_solver_ref.cubin")
 REF_CUBIN_NOFMA = os.path.join(REF_OUT, "gpu_solver_ref_nofma.cubin")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -89,6 +93,42 @@ def build_ref(force: bool = False) -> list[str]:
     return out
 
 
+REF_CPU_LIB = os.path.join(REF_OUT, "libpfref_cpu.so")
+REF_CPU_SOURCES = ["phase_field.cpp", "solver.cpp", "thermo_data.cpp", "thermo_functor.cpp", "write_data.cpp"]
+
+
+def build_ref_cpu(force: bool = False) -> str | None:
+    """Compile the reference's own CPU time step into oracle/_ref/libpfref_cpu.so.
+
+    The unmodified sources C++-openmp-cuda/src/{phase_field,solver,thermo_data,
+    thermo_functor,write_data}.cpp are compiled straight from the read-only
+    checkout against oracle/blitz_shim (a minimal stand-in for the Blitz++
+    Array API they use), together with ref_cpu_runner.cpp (C entry points and
+    "no GPU" stubs for gpu_solver.h).  -ffp-contract=off keeps the reference's
+    x86 build semantics (no fused multiply-add) on every host.  Returns None
+    where the checkout is absent (the library is then used only if it exists).
+    """
+    srcs = [os.path.join(REF_SRC, f) for f in REF_CPU_SOURCES]
+    if not all(os.path.exists(p) for p in srcs):
+        return REF_CPU_LIB if os.path.exists(REF_CPU_LIB) else None
+    os.makedirs(REF_OUT, exist_ok=True)
+    shim = os.path.join(HERE, "blitz_shim")
+    runner = os.path.join(HERE, "ref_cpu_runner.cpp")
+    deps = srcs + [runner, os.path.join(shim, "blitz", "array.h"), __file__]
+    if force or _newer(REF_CPU_LIB, deps):
+        # phase_field::Read_data hands system() a pointer into a destroyed
+        # temporary string (phase_field.cpp:47-49), so the shell runs whatever
+        # that memory holds; the linker's --wrap sends the call to a no-op in
+        # the runner (the caller creates the output directory itself).
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+               "-w", "-Wl,--wrap=system", "-I", shim, "-I", REF_SRC] + srcs + [runner, "-o", REF_CPU_LIB]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference CPU build failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
+    return REF_CPU_LIB
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_ref())
+    print(build_ref_cpu())

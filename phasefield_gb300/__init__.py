@@ -27,6 +27,7 @@ PF_ERR_NONFINITE = -5
 PF_ERR_IO = -6
 PF_ERR_NODEV = -7
 PF_ERR_RANGE = -8
+PF_ERR_DRIFT = -9
 PF_PREC_FP64 = 0
 PF_PREC_FP32C = 1
 PF_MAXT = 64
@@ -295,7 +296,7 @@ class PhaseField:
         return out
 
     def check_state(self, reference_totals=None, max_rel_drift: float = 0.0) -> int:
-        """Status of pf_check_state (PF_OK or PF_ERR_NONFINITE), without raising."""
+        """Status of pf_check_state (PF_OK, PF_ERR_NONFINITE or PF_ERR_DRIFT), without raising."""
         ref = None if reference_totals is None else np.ascontiguousarray(reference_totals, np.float64)
         return lib().pf_check_state(self._ctx, None if ref is None else ref.ctypes.data_as(_DP), max_rel_drift, None)
 

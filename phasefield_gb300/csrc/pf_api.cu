@@ -139,6 +139,11 @@ struct pf_ctx {
     int *d_span = nullptr;
     unsigned int *d_trunc = nullptr;
     long long truncated = 0;
+    // Reference-layout (FP64) staging buffers of the FP32C upload/download,
+    // allocated on first use and kept until pf_destroy, so repeated uploads
+    // and downloads allocate nothing.
+    int *st_ids = nullptr;
+    double *st_phi = nullptr, *st_phase = nullptr, *st_C = nullptr, *st_conc = nullptr;
     // reductions
     double *partials = nullptr;
     int red_blocks = 0;
@@ -214,6 +219,7 @@ void free_all(pf_ctx *c) {
     }
     cudaFree(c->phase); cudaFree(c->C); cudaFree(c->phase32);
     cudaFree(c->d_span); cudaFree(c->d_trunc);
+    cudaFree(c->st_ids); cudaFree(c->st_phi); cudaFree(c->st_phase); cudaFree(c->st_C); cudaFree(c->st_conc);
     cudaFree(c->partials); cudaFree(c->d_red);
     if (c->h_red) cudaFreeHost(c->h_red);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -263,6 +269,25 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         }
     }
     return e;
+}
+
+// The FP32C context's reference-layout staging buffers (conc only when asked).
+bool ensure_staging(pf_ctx *c, bool conc) {
+    const size_t N = (size_t)c->N;
+    bool ok = true;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (ok && !*p && cudaMalloc(p, bytes) != cudaSuccess) {
+            *p = nullptr;
+            ok = false;
+        }
+    };
+    alloc((void **)&c->st_ids, 6 * N * sizeof(int));
+    alloc((void **)&c->st_phi, 6 * N * sizeof(double));
+    alloc((void **)&c->st_phase, 3 * N * sizeof(double));
+    alloc((void **)&c->st_C, N * c->nsol * sizeof(double));
+    if (conc) alloc((void **)&c->st_conc, 3 * N * c->nsol * sizeof(double));
+    if (!ok) cudaGetLastError();
+    return ok;
 }
 
 bool same_step(const pf_step_params &a, const pf_step_params &b) {
@@ -375,20 +400,12 @@ extern "C" int pf_upload_state(pf_ctx *c, const int32_t *ids, const double *phi,
         else
             PF_CUDA_OK(pf_launch_partition_f64(P, c->phase, c->C, c->conc[0], c->stream));
     } else {
-        // Stage the reference layout in the (not yet used) second buffers'
-        // space: FP64 staging buffers are allocated for the duration of the
-        // upload only.
-        int *d_ids = nullptr;
-        double *d_phi = nullptr, *d_phase = nullptr, *d_C = nullptr;
-        bool ok = cudaMalloc(&d_ids, 6 * N * sizeof(int)) == cudaSuccess &&
-                  cudaMalloc(&d_phi, 6 * N * sizeof(double)) == cudaSuccess &&
-                  cudaMalloc(&d_phase, 3 * N * sizeof(double)) == cudaSuccess &&
-                  cudaMalloc(&d_C, N * c->nsol * sizeof(double)) == cudaSuccess;
+        // The reference layout is staged in the context's FP64 buffers and
+        // packed on the device.
         int st = PF_OK;
-        if (!ok) {
-            cudaGetLastError();
-            st = pf_fail(PF_ERR_NOMEM, "pf_upload_state: staging allocation failed");
-        }
+        if (!ensure_staging(c, false)) st = pf_fail(PF_ERR_NOMEM, "pf_upload_state: staging allocation failed");
+        int *d_ids = c->st_ids;
+        double *d_phi = c->st_phi, *d_phase = c->st_phase, *d_C = c->st_C;
         cudaError_t e = cudaSuccess;
         if (st == PF_OK) {
             cudaMemcpyAsync(d_ids, ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
@@ -423,7 +440,6 @@ extern "C" int pf_upload_state(pf_ctx *c, const int32_t *ids, const double *phi,
             }
         }
         cudaStreamSynchronize(c->stream);
-        cudaFree(d_ids); cudaFree(d_phi); cudaFree(d_phase); cudaFree(d_C);
         if (st != PF_OK) return st;
     }
     c->have_state = true;
@@ -447,18 +463,13 @@ extern "C" int pf_download_state(pf_ctx *c, int32_t *ids, double *phi, double *p
         PF_CUDA_OK(cudaStreamSynchronize(c->stream));
         return PF_OK;
     }
-    int *d_ids = nullptr;
-    double *d_phi = nullptr, *d_phase = nullptr, *d_conc = nullptr, *d_C = nullptr;
-    bool ok = cudaMalloc(&d_ids, 6 * N * sizeof(int)) == cudaSuccess &&
-              cudaMalloc(&d_phi, 6 * N * sizeof(double)) == cudaSuccess &&
-              cudaMalloc(&d_phase, 3 * N * sizeof(double)) == cudaSuccess &&
-              cudaMalloc(&d_C, N * c->nsol * sizeof(double)) == cudaSuccess &&
-              (!conc || cudaMalloc(&d_conc, 3 * N * c->nsol * sizeof(double)) == cudaSuccess);
     int st = PF_OK;
-    if (!ok) {
-        cudaGetLastError();
+    if (!ensure_staging(c, conc != nullptr)) {
         st = pf_fail(PF_ERR_NOMEM, "pf_download_state: staging allocation failed");
     } else {
+        int *d_ids = c->st_ids;
+        double *d_phi = c->st_phi, *d_phase = c->st_phase, *d_C = c->st_C;
+        double *d_conc = conc ? c->st_conc : nullptr;
         pf_step_params P;
         pf_compute_params(c->model, c->time, P);
         cudaError_t e = pf_launch_unpack_f32(P, c->map, c->gid[c->cur], c->phi32[c->cur], c->phase32, c->sol[c->curs],
@@ -474,7 +485,6 @@ extern "C" int pf_download_state(pf_ctx *c, int32_t *ids, double *phi, double *p
         if (e != cudaSuccess) st = pf_cuda_fail(e);
     }
     cudaStreamSynchronize(c->stream);
-    cudaFree(d_ids); cudaFree(d_phi); cudaFree(d_phase); cudaFree(d_conc); cudaFree(d_C);
     return st;
 }
 
@@ -614,8 +624,8 @@ extern "C" int pf_set_diffusion_tile(pf_ctx *c, int ty, int zchunk, int variant)
         c->diff_cfg_valid = false;
         return PF_OK;
     }
-    if ((ty != 4 && ty != 8 && ty != 16) || zchunk < 1 || variant < 0 || variant > 1)
-        return pf_fail(PF_ERR_ARG, "pf_set_diffusion_tile: tile height 4/8/16, z chunk >= 1, variant 0/1");
+    if ((ty != 4 && ty != 8 && ty != 16) || zchunk < 1 || variant != 0)
+        return pf_fail(PF_ERR_ARG, "pf_set_diffusion_tile: tile height 4/8/16, z chunk >= 1, variant 0");
     c->diff_cfg = pf_diff_cfg{ty, zchunk, variant};
     c->diff_cfg_valid = true;
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
@@ -668,7 +678,7 @@ extern "C" int pf_check_state(pf_ctx *c, const double reference_totals[2], doubl
         for (int q = 0; q < c->nsol; q++) {
             const double ref = reference_totals[q];
             if (ref != 0.0 && std::abs(r[4 + q] - ref) > max_rel_drift * std::abs(ref))
-                return pf_fail(PF_ERR_NONFINITE, "pf_check_state: solute total drifted beyond the tolerance");
+                return pf_fail(PF_ERR_DRIFT, "pf_check_state: solute total drifted beyond the tolerance");
         }
     return PF_OK;
 }

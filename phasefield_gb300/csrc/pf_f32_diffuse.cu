@@ -265,13 +265,12 @@ cudaError_t launch_one(const pf_f32_params &P, const float *sphase, const float2
     using S = Smem<NSOL, TX, TY>;
     const int tiles = ((P.ix + TX - 1) / TX) * ((P.iy + TY - 1) / TY);
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(S));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // The shared-memory opt-in is a per-device, per-context attribute: set it
+    // on every launch (a host-side driver call, far below the kernel's time) so
+    // a second device or a re-created context is never launched without it.
+    cudaError_t e = cudaFuncSetAttribute(k_diffuse<NSOL, NNB, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(S));
+    if (e != cudaSuccess) return e;
     k_diffuse<NSOL, NNB, TX, TY><<<grid, TX * TY, sizeof(S), s>>>(P, sphase, sol_in, sol_out, zchunk);
     return cudaGetLastError();
 }

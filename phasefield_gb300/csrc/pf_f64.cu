@@ -270,12 +270,14 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
     ph[0] = __ldg(phase + 3 * n + 0);
     ph[1] = __ldg(phase + 3 * n + 1);
     ph[2] = __ldg(phase + 3 * n + 2);
-    double nph[6][3];
+    // Flux weights sqrt(phase_p^nb * phase_p) (solver.cpp:363) do not depend on
+    // the solute: evaluated once per cell, not once per solute.
+    double w[6][3];
 #pragma unroll
     for (int b = 0; b < 6; b++)
         if (b < nnb) {
 #pragma unroll
-            for (int p = 0; p < 3; p++) nph[b][p] = __ldg(phase + 3 * nbr[b] + p);
+            for (int p = 0; p < 3; p++) w[b][p] = sqrt(__ldg(phase + 3 * nbr[b] + p) * ph[p]);
         }
     for (int q = 0; q < P.nsol; q++) {
         const double *c1 = conc1 + (long long)q * 3 * P.N;
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
             if (b < nnb) {
 #pragma unroll
                 for (int p = 0; p < 3; p++)
-                    del += sqrt(nph[b][p] * ph[p]) * (__ldg(c1 + 3 * nbr[b] + p) - cs[p]) * P.D[q][p];
+                    del += w[b][p] * (__ldg(c1 + 3 * nbr[b] + p) - cs[p]) * P.D[q][p];
             }
         del *= coef;
         const double cn = C[q * P.N + n] + del;

@@ -51,6 +51,7 @@ extern "C" const char *pf_status_string(int s) {
         case PF_ERR_IO: return "file error";
         case PF_ERR_NODEV: return "no CUDA device";
         case PF_ERR_RANGE: return "value out of range";
+        case PF_ERR_DRIFT: return "solute total drifted";
         default: return "unknown status";
     }
 }

@@ -37,7 +37,7 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
 struct pf_diff_cfg {
     int ty;
     int zchunk;
-    int variant; // 0: two barriers per plane; 1: double-buffered records, one barrier
+    int variant; // 0: one sub-step per pass over the grid
 };
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P);
 int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max);

@@ -15,7 +15,9 @@
 // memory, silently use the wrong memory.  The device address is therefore
 // taken with cudaGetSymbolAddress once per device, with that device current,
 // the first time the entry point runs on it; that first call should come
-// before any stream capture.
+// before any stream capture.  The address is kept for the life of the process:
+// cudaDeviceReset unloads the module, so the entry point is not to be called
+// on a device after that device has been reset.
 //
 // All calls share the one array and it keeps the last call's contents.  The
 // completion counter is cleared on the call's stream before the kernel runs and

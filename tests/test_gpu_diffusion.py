@@ -60,7 +60,7 @@ def test_every_tile_candidate_gives_the_same_answer(gpu, tmp_path, grid):
     F = pf.PhaseField(m, pf.PF_PREC_FP32C)
     F.upload(st0, 0.0)
     cands = F.diffusion_candidates()
-    assert {c[2] for c in cands} == {0, 1}
+    assert len(cands) >= 3 and {c[2] for c in cands} <= {0}
     for ty, zc, var in cands:
         F.upload(st0, 0.0)
         F.set_diffusion_tile(ty, zc, var)

@@ -20,7 +20,8 @@ def test_nonfinite_and_drift_are_reported(gpu, tmp_path, prec):
     F.update(3)
     totals = [st["C"][:N].sum(), st["C"][N:].sum()]
     assert F.check_state(totals, 1e-6) == pf.PF_OK
-    assert F.check_state([totals[0] * 1.01, totals[1]], 1e-6) == pf.PF_ERR_NONFINITE  # drift beyond tolerance
+    assert F.check_state([totals[0] * 1.01, totals[1]], 1e-6) == pf.PF_ERR_DRIFT  # drift beyond tolerance
+    assert b"drifted" in pf.lib().pf_last_error()
     bad = {k: v.copy() for k, v in st.items()}
     bad["C"][17] = np.nan
     F.upload(bad, 0.0)
@@ -34,6 +35,7 @@ def test_bad_arguments_are_refused(gpu, tmp_path):
     assert pf.lib().pf_step(F._ctx, 1) == pf.PF_ERR_ARG          # no state uploaded
     assert pf.lib().pf_step(F._ctx, -1) == pf.PF_ERR_ARG
     assert pf.lib().pf_set_diffusion_tile(F._ctx, 5, 8, 0) == pf.PF_ERR_ARG
+    assert pf.lib().pf_set_diffusion_tile(F._ctx, 8, 8, 7) == pf.PF_ERR_ARG      # unknown kernel variant
     bad = pf.PfModel()
     bad.ix = 0
     h = pf.ctypes.c_void_p()

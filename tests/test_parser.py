@@ -11,7 +11,9 @@ import phasefield_gb300 as pf
 import pyoracle as po
 from phasefield_gb300 import workloads as W
 
-REF_BUILD = "/root/reference/C++-openmp-cuda/build"
+from build_oracle import REF_ROOT
+
+REF_BUILD = os.path.join(REF_ROOT, "C++-openmp-cuda", "build")
 
 
 def _same(m: pf.PfModel, d: dict):

@@ -56,6 +56,34 @@ def test_reduce_noalloc_matches_pf_reduce(gpu, tmp_path):
         assert got[7] == 0.0
 
 
+def test_reduce_noalloc_allocates_nothing(gpu, tmp_path):
+    """After a first call on the device (which loads the library's module and
+    looks up the scratch address), repeated calls leave the device's free
+    memory exactly unchanged: the entry point allocates nothing."""
+    import torch
+
+    L = pf.lib()
+    m, st, expected = _state_and_expected(tmp_path, (24, 20, 10), 2, 3)
+    N = m.ix * m.iy * m.iz
+    d = {k: torch.from_numpy(st[k]).cuda() for k in ("ids", "phi", "phase", "C")}
+    out = torch.zeros(8, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def call():
+        return L.pf_reduce_noalloc(N, m.nsol, d["ids"].data_ptr(), d["phi"].data_ptr(), d["phase"].data_ptr(),
+                                   d["C"].data_ptr(), out.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+
+    assert call() == pf.PF_OK, L.pf_last_error()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        assert call() == pf.PF_OK, L.pf_last_error()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0
+    np.testing.assert_allclose(out.cpu().numpy(), expected, rtol=1e-12, atol=1e-12)
+
+
 def test_reduce_noalloc_rejects_oversize(gpu):
     import torch
 
