@@ -1,10 +1,10 @@
 """Benchmark of the Steinbach multi-phase-field time step on GB300.
 
-Workload (default): the 3D FP32-compensated configuration -- 256^3 cells,
-200 Voronoi ferrite grains + 2000 austenite nuclei (radius 2 cells), up to 4
-active grains per cell, C 0.10 / Mn 1.5 wt% with +-0.02 wt% uniform noise,
-T = 1013 K.  One "step" is one full time step: the phase sweep plus n_sub
-diffusion sub-steps (n_sub = 10 at 1013 K).
+Workload (default): the large 3D production configuration -- 512^3 cells,
+1000 Voronoi ferrite grains + 20000 austenite nuclei (radius 2 cells), up to 4
+active grains per cell (uint16 ids, FP32 fractions), C 0.10 / Mn 1.5 wt%,
+T = 1023 K.  One "step" is one full time step: the phase sweep plus n_sub
+diffusion sub-steps.  ``--workload 3d256`` selects the 256^3 configuration.
 
 Printed JSON (rank 0, one line):
   value    cell-updates/s of the FP32-compensated step with the state resident
@@ -15,14 +15,17 @@ Printed JSON (rank 0, one line):
   roofline the diffusion sub-step kernel (the dominant one): algorithmic bytes
            per launch / mean launch time (CUDA events around each launch).
   fp64     the plain FP64 step (reference layout) on the same workload.
-  cpu_baseline  the FP64 CPU oracle on a bounded sample of the workload.
+  cpu_baseline  the FP64 CPU oracle (bit-for-bit equal to the reference's own
+           CPU code on the golden cases) on a bounded sample of the workload: a
+           slab of the same initial state.
 
---impl reference times the reference's CPU algorithm (the FP64 oracle, a
-restatement of the reference's OpenMP solver, which itself cannot be built here)
-on the host cores over the same workload, one bounded sample per step.
+--impl reference times the reference's CPU algorithm (the FP64 oracle) on all
+host cores over the same workload and configuration, one bounded sample per
+step (a z slab of the same seeded state, generated by the oracle library's own
+copy of the input generator; the product library is not loaded).
 
-Multi-GPU (--gpus N under torchrun): the path does not shard for one domain in
-this build, so each rank advances an independent replica (different seed);
+Multi-GPU (--gpus N under torchrun): one domain does not shard in this build,
+so each rank advances an independent replica (different seed);
 value = all ranks' cells x steps / max-over-ranks time ("scaling": "weak").
 """
 from __future__ import annotations
@@ -42,6 +45,12 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "cell-updates/s & % HBM roofline: FP32 vs FP64 step; batch; adjoint/fwd ratio"
+_T0 = time.perf_counter()
+
+
+def _log(msg: str) -> None:
+    """Progress of the legs on stderr (the JSON line goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
 UNIT = "cell-updates/s"
 
 
@@ -138,33 +147,58 @@ def _scaled_spec(wl, grid):
     return s
 
 
-def cpu_sample(wl, threads: int | None = None):
-    """FP64 oracle on a bounded sample of the workload: returns (model, state, time, cells, label)."""
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import phasefield_gb300 as pf
-    import pyoracle as po
-
-    gx, gy, gz = wl.grid
-    grid = (gx, gy, max(1, min(gz, 32))) if gz > 1 else (gx, gy, 1)
-    cfg, m = _model_for(wl, grid)
-    om = po.load_model(cfg)
-    st = pf.init_microstructure(m, _scaled_spec(wl, grid), 0.0)
-    if threads:
-        po.set_threads(threads)
-    label = (f"{grid[0]}x{grid[1]}x{grid[2]} periodic box of the {wl.name} workload (same grain/nucleus density), "
-             f"one FP64 step per sample")
-    return om, st, grid[0] * grid[1] * grid[2], label
+def _config(wl, grid, n_sub: int, nsol: int) -> dict:
+    """The workload description both arms print (identical by construction)."""
+    return {"workload": f"{wl.name}: {grid[0]}x{grid[1]}x{grid[2]} cells, {wl.n_grains} grains, "
+                        f"{wl.n_nuclei} nuclei r={wl.nucleus_radius}, C/Mn {wl.C0} +-{wl.C_noise[0]} wt%, "
+                        f"T={wl.T} K, n_sub={n_sub}",
+            "grid": list(grid), "n_sub": n_sub, "solutes": nsol,
+            "l2": f"inputs larger than L2 (FP32 state {grid[0] * grid[1] * grid[2] * 52 / 1e9:.2f} GB, L2 0.13 GB)"}
 
 
-def run_reference(args) -> dict:
-    """--impl reference: the reference's CPU algorithm (FP64 oracle) on the host cores."""
+SLAB_PLANES = 32
+
+
+def cpu_sample(wl, grid):
+    """A bounded sample of the workload for the FP64 CPU oracle, built without
+    the product library: planes [z0, z0 + SLAB_PLANES) of the workload's own
+    seeded initial state (the oracle library carries the same input
+    generator), stepped as a periodic box.  Returns (oracle model, state,
+    cells per step, n_sub, label)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import build_oracle
     import pyoracle as po
+    from phasefield_gb300 import workloads as W
 
     build_oracle.build_oracle()
+    d = tempfile.mkdtemp(prefix="pfcpu_")
+    W.write_thermo(os.path.join(d, "thermo_steel.txt"))
+    full_cfg = W.write_config(os.path.join(d, "full.txt"), grid=grid, dx=wl.dx, T=wl.T, directory=d)
+    om_full = po.load_model(full_cfg)
+    nz = min(SLAB_PLANES, grid[2])
+    z0 = (grid[2] - nz) // 2
+    spec = wl.spec() if tuple(grid) == tuple(wl.grid) else _scaled_spec(wl, grid)
+    st = po.init_state(om_full, spec, 0.0, z0=z0, nz=nz)
+    slab_cfg = W.write_config(os.path.join(d, "slab.txt"), grid=(grid[0], grid[1], nz), dx=wl.dx, T=wl.T,
+                              directory=d)
+    om = po.load_model(slab_cfg)
+    n_sub = po.params_at(om_full, 0.0).n_sub
+    cells = grid[0] * grid[1] * nz
+    label = (f"planes {z0}..{z0 + nz - 1} of the {wl.name} seeded initial state ({grid[0]}x{grid[1]}x{nz} cells, "
+             f"same state as the GPU arm), stepped as a periodic box; one full FP64 time step (phase sweep + "
+             f"n_sub={n_sub} diffusion sub-steps) per sample")
+    return om, st, cells, n_sub, label
+
+
+def run_reference(args) -> dict:
+    """--impl reference: the reference's CPU algorithm (FP64 oracle) on the host
+    cores, over the same workload and configuration as the GPU arm."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle as po
+
     wl = _workload(args.workload)
-    om, st, cells, label = cpu_sample(wl)
+    grid = tuple(args.grid) if args.grid else wl.grid
+    om, st, cells, n_sub, label = cpu_sample(wl, grid)
     t = 0.0
     for _ in range(args.warmup):
         t = po.run(om, st, t, 1)
@@ -177,7 +211,7 @@ def run_reference(args) -> dict:
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Voronoi grains + nuclei)",
-        "config": {"workload": wl.name, "sample": label},
+        "config": _config(wl, grid, n_sub, om.nsol),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": label},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -259,52 +293,69 @@ def run_adjoint(args) -> dict:
 
 
 def run_precision(args) -> dict:
-    """Error of the FP32-compensated path against FP64 on a 128^3 box of the 3D
-    workload (same grain/nucleus densities) after --precision-steps steps:
-    against the four-slot model in FP64 (the calibration model: isolates FP32
-    rounding) and against the six-slot FP64 reference path (adds the model
-    change of keeping four grains per cell)."""
+    """Error of the FP32-compensated path against FP64 on the 3D FP32-vs-FP64
+    configuration (3d256: 256^3, 200 grains, 2000 nuclei, T = 1013 K, 2000
+    steps; --precision-grid scales the box keeping grain and nucleus densities):
+    against the four-slot model in FP64 (the workload's own model -- up to 4
+    grains per cell -- so the difference is FP32 rounding alone), and, on a
+    --six-slot-grid box, against the six-slot FP64 reference path (which adds
+    the model change of keeping four grains per cell)."""
     import numpy as np
 
     import phasefield_gb300 as pf
+    from phasefield_gb300 import workloads as W
 
-    wl = _workload(args.workload)
-    grid = (128, 128, 128) if wl.grid[2] > 1 else (256, 256, 1)
-    cfg, m = _model_for(wl, grid)
-    st = pf.init_microstructure(m, _scaled_spec(wl, grid), 0.0)
-    N = grid[0] * grid[1] * grid[2]
+    wl = W.WORKLOADS["3d256"]
     S = args.precision_steps
-    F32 = pf.PhaseField(m, pf.PF_PREC_FP32C)
-    F32.upload(st, 0.0)
-    F32.update(S)
-    a32 = F32.download(conc=False)
-    r32 = F32.reduce()
-    F32.close()
-    F64 = pf.PhaseField(m, pf.PF_PREC_FP64)
-    F64.upload(st, 0.0)
-    F64.update(S)
-    a64 = F64.download(conc=False)
-    F64.close()
-    A = pf.Adjoint(m, pf.PF_PREC_FP64, max(S, 1))
-    A.upload(st, 0.0)
-    A.forward(S)
-    a4 = A.final_state()
-    A.close()
 
-    def err(ref_phase, ref_C):
+    def setup(g):
+        grid = (g, g, g)
+        cfg, m = _model_for(wl, grid)
+        spec = wl.spec() if grid == wl.grid else _scaled_spec(wl, grid)
+        return m, pf.init_microstructure(m, spec, 0.0), g * g * g
+
+    def fp32(m, st):
+        F = pf.PhaseField(m, pf.PF_PREC_FP32C)
+        F.upload(st, 0.0)
+        F.update(S)
+        out = F.download(conc=False)
+        out["reduce"] = F.reduce()
+        F.close()
+        return out
+
+    def err(a32, ref_phase, ref_C, N):
         d = np.abs(a32["phase"] - ref_phase)
         fr32 = a32["phase"].reshape(N, 3).mean(0)
         frr = ref_phase.reshape(N, 3).mean(0)
         return {"phase_max_abs": float(d.max()), "phase_mean_abs": float(d.mean()),
                 "cells_phase_err_gt_1e-5": int((d.reshape(N, 3).max(1) > 1e-5).sum()),
                 "carbon_max_rel": float(np.max(np.abs(a32["C"][:N] - ref_C) / np.abs(ref_C))),
+                "carbon_mean_rel": float(np.mean(np.abs(a32["C"][:N] - ref_C) / np.abs(ref_C))),
                 "phase_fraction_abs": [float(x) for x in np.abs(fr32 - frr)]}
 
+    t0 = time.perf_counter()
+    m, st, N = setup(args.precision_grid)
+    a32 = fp32(m, st)
+    A = pf.Adjoint(m, pf.PF_PREC_FP64, max(S, 1))
+    A.upload(st, 0.0)
+    A.forward(S)
+    a4 = A.final_state()
+    A.close()
     C0 = st["C"][:N].sum()
-    return {"grid": list(grid), "steps": S, "cells": N,
-            "vs_fp64_four_slot": err(a4["phase"], a4["C"]),
-            "vs_fp64_six_slot": err(a64["phase"], a64["C"][:N]),
-            "carbon_mass_rel_drift_fp32": float(abs(r32[4] - C0) / C0)}
+    out = {"grid": [args.precision_grid] * 3, "steps": S, "cells": N,
+           "vs_fp64_four_slot": err(a32, a4["phase"], a4["C"], N),
+           "carbon_mass_rel_drift_fp32": float(abs(a32["reduce"][4] - C0) / C0)}
+    if args.six_slot_grid > 0:
+        m6, st6, N6 = setup(args.six_slot_grid)
+        b32 = fp32(m6, st6)
+        F64 = pf.PhaseField(m6, pf.PF_PREC_FP64)
+        F64.upload(st6, 0.0)
+        F64.update(S)
+        a64 = F64.download(conc=False)
+        F64.close()
+        out["vs_fp64_six_slot"] = dict(err(b32, a64["phase"], a64["C"][:N6], N6), grid=[args.six_slot_grid] * 3)
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
@@ -318,9 +369,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     wl = _workload(args.workload)
     grid = tuple(args.grid) if args.grid else wl.grid
     cfg, m = _model_for(wl, grid)
-    spec = _scaled_spec(wl, grid) if args.grid else wl.spec()
+    spec = wl.spec() if tuple(grid) == tuple(wl.grid) else _scaled_spec(wl, grid)
     spec.seed = wl.seed + rank
+    _log(f"initial state {grid}")
     st0 = pf.init_microstructure(m, spec, 0.0)
+    _log("initial state done")
     N = grid[0] * grid[1] * grid[2]
     P = pf.params_at(m, 0.0)
     nsol = m.nsol
@@ -365,6 +418,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     F.enable_kernel_timing(False)
     F.close()
 
+    _log("FP32C leg done")
     # ---- FP64 plain step on the same workload ----------------------------
     fp64 = None
     if args.fp64_steps > 0:
@@ -390,6 +444,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     if args.no_e2e:
         return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk, tuned)
 
+    _log("FP64 leg done")
     # ---- e2e: through the C ABI with pinned host buffers -----------------
     keep_alive = []
 
@@ -440,13 +495,14 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
     ach = diff_bytes / t_diff / 1e9
     step_bytes = phase_bytes + P.n_sub * diff_bytes
 
+    _log("e2e leg done")
     # ---- CPU baseline (oracle, bounded sample) ----------------------------
     cpu = None
     if not args.no_cpu:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import pyoracle as po
 
-        om, cst, cells, label = cpu_sample(wl)
+        om, cst, cells, _, label = cpu_sample(wl, grid)
         tcur = po.run(om, cst, 0.0, 1)
         c0 = time.perf_counter()
         nst = 2
@@ -472,12 +528,7 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 (Kahan-compensated solutes, fp64 reductions)",
         "data": "synthetic (seeded Voronoi grains + nuclei, uniform noise)",
-        "config": {"workload": f"{wl.name}: {grid[0]}x{grid[1]}x{grid[2]} cells, {wl.n_grains} grains, "
-                               f"{wl.n_nuclei} nuclei r={wl.nucleus_radius}, C/Mn {wl.C0} +-{wl.C_noise[0]} wt%, "
-                               f"T={wl.T} K, n_sub={P.n_sub}",
-                   "grid": list(grid), "n_sub": P.n_sub, "solutes": nsol,
-                   "l2": f"inputs larger than L2 (FP32 state {N * 52 / 1e9:.2f} GB, L2 0.13 GB)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": _config(wl, grid, P.n_sub, nsol),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
                      "kernel": "k_diffuse_f32",
@@ -507,14 +558,17 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="3d256")
-    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--workload", default="3d512")
+    ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the diffusion tile autotuner")
-    ap.add_argument("--batch-steps", type=int, default=1000, help="steps of the 64-domain ensemble (0 = skip)")
+    ap.add_argument("--batch-steps", type=int, default=5000, help="steps of the 64-domain ensemble (0 = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint calibration run (0 = skip)")
     ap.add_argument("--precision-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 error run (0 = skip)")
+    ap.add_argument("--precision-grid", type=int, default=256, help="cube side of the FP32-vs-FP64 error run")
+    ap.add_argument("--six-slot-grid", type=int, default=128,
+                    help="cube side of the FP32C-vs-six-slot-FP64 comparison (0 = skip)")
     ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -539,14 +593,18 @@ def main() -> None:
         if rank != 0:
             __graft_entry__.build()
     out = run_ours(args, rank, world, local_rank)
+    _log("main leg done")
     if args.batch_steps > 0:
         b = run_batch(args, rank)
+        _log("batch done")
         if out is not None:
             out["batch"] = b
     if args.adjoint_steps > 0 and out is not None:
         out["adjoint"] = run_adjoint(args)
+        _log("adjoint done")
     if args.precision_steps > 0 and out is not None:
         out["precision"] = run_precision(args)
+        _log("precision done")
     if out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:

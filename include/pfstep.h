@@ -166,6 +166,10 @@ int pf_params_at(const pf_model *model, double time, pf_step_params *out);
 /* Fill host arrays (reference layout) with a seeded initial state at 'time'. */
 int pf_init_microstructure(const pf_model *model, const pf_init_spec *spec, double time, int32_t *ids,
                            double *phi, double *phase, double *conc, double *C);
+/* The same state restricted to planes [z0, z0+nz) of the model's grid (arrays
+ * sized for ix*iy*nz cells): equal to those planes of the whole domain. */
+int pf_init_microstructure_box(const pf_model *model, const pf_init_spec *spec, double time, int z0, int nz,
+                               int32_t *ids, double *phi, double *phase, double *conc, double *C);
 
 typedef struct pf_ctx pf_ctx;
 int pf_create(const pf_model *model, int precision, pf_ctx **out);

@@ -3,7 +3,9 @@
 * ``build_oracle()`` compiles the FP64 CPU oracle ``pf_oracle.c`` into
   ``oracle/_build/liboracle.so`` with ``-ffp-contract=off`` (no fused
   multiply-add, so its rounding matches the product's FP64 GPU path and the
-  reference's host arithmetic) and OpenMP.
+  reference's host arithmetic) and OpenMP, together with the seeded input
+  generator (``phasefield_gb300/csrc/pf_init.cpp``) so the CPU baseline can
+  build its input state without loading the product library.
 * ``build_ref()`` compiles the reference's own CUDA diffusion plug-in,
   ``C++-openmp-cuda/src/gpu_solver.cpp`` from the read-only reference checkout,
   into device-only cubins under ``oracle/_ref/`` (one with the default
@@ -41,15 +43,30 @@ def _newer(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+REPO = os.path.dirname(HERE)
+# The seeded input generator is one source file shared with the product, so
+# the CPU baseline steps exactly the state the GPU steps (it generates inputs;
+# it is not part of what is checked).
+INIT_SRC = os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init.cpp")
+INIT_HDRS = [os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init.h"), os.path.join(REPO, "include", "pfstep.h")]
+
+
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     src = [os.path.join(HERE, "pf_oracle.c"), os.path.join(HERE, "pf_oracle.h")]
-    if force or _newer(LIB, src + [__file__]):
-        cmd = ["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-               "-fno-fast-math", src[0], "-o", LIB, "-lm"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+    if force or _newer(LIB, src + [INIT_SRC] + INIT_HDRS + [__file__]):
+        o1 = os.path.join(BUILD, "pf_oracle.o")
+        o2 = os.path.join(BUILD, "pf_init.o")
+        inc = ["-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "phasefield_gb300", "csrc")]
+        cmds = [["gcc", "-O3", "-std=c99", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-c", src[0],
+                 "-o", o1],
+                ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"] + inc +
+                ["-c", INIT_SRC, "-o", o2],
+                ["g++", "-shared", "-fopenmp", o1, o2, "-o", LIB, "-lm"]]
+        for cmd in cmds:
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
     return LIB
 
 

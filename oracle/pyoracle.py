@@ -55,6 +55,16 @@ class OParams(ctypes.Structure):
     ]
 
 
+class OInitSpec(ctypes.Structure):
+    """Layout of pf_init_spec (include/pfstep.h): the seeded input generator's spec."""
+    _fields_ = [
+        ("seed", ctypes.c_uint64), ("n_grains", ctypes.c_int), ("n_nuclei", ctypes.c_int),
+        ("nucleus_radius", ctypes.c_double), ("n_particles", ctypes.c_int), ("particle_radius", ctypes.c_double),
+        ("width", ctypes.c_double), ("C0", ctypes.c_double * 2), ("C_noise", ctypes.c_double * 2),
+        ("max_slots", ctypes.c_int),
+    ]
+
+
 class OState(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("ids1", "ids2", "phi1", "phi2", "phase", "conc1", "conc2", "C")]
 
@@ -83,6 +93,10 @@ def lib() -> ctypes.CDLL:
         L.pfo_fractions.argtypes = [M, _P, _P, _P, _P]
         L.pfo_temperature.argtypes = [M, _D]
         L.pfo_temperature.restype = _D
+        L.pf_init_state.argtypes = [ctypes.c_int] * 4 + [_D, ctypes.POINTER(OInitSpec), _P, _P, ctypes.c_int,
+                                                          ctypes.c_int, _P, _P, _P, _P, _P,
+                                                          ctypes.POINTER(ctypes.c_char_p)]
+        L.pf_init_state.restype = ctypes.c_int
         L.pfo_num_threads.restype = ctypes.c_int
         L.pfo_set_num_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -327,6 +341,37 @@ def ref_gpu_diffusion_solver(variant, D3, k9, c9, phase, C, x, y, z, dt, dx) -> 
     if n < 0:
         raise RuntimeError("reference kernels: " + _runner.ref_last_error().decode())
     return n
+
+
+def init_state(m: OModel, spec, time: float, grid=None, z0: int = 0, nz: int | None = None) -> dict:
+    """The seeded input state (reference layout) of planes [z0, z0+nz) of the
+    periodic domain 'grid' (default: the model's grid), generated by the same
+    source as the product's pf_init_microstructure.  'spec' is any object with
+    the fields of pf_init_spec.  conc is partitioned with the model's
+    parameters at 'time'."""
+    ix, iy, iz = grid if grid is not None else (m.ix, m.iy, m.iz)
+    nz = iz - z0 if nz is None else nz
+    s = OInitSpec()
+    for f, _ in OInitSpec._fields_:
+        v = getattr(spec, f)
+        if f in ("C0", "C_noise"):
+            for q in range(2):
+                getattr(s, f)[q] = v[q]
+        else:
+            setattr(s, f, v)
+    p = params_at(m, time)
+    k = np.array([[p.k[q][e] for e in range(9)] for q in range(2)], np.float64)
+    c = np.array([[p.c[q][e] for e in range(9)] for q in range(2)], np.float64)
+    N = ix * iy * nz
+    st = {"ids": np.zeros(6 * N, np.int32), "phi": np.zeros(6 * N, np.float64), "phase": np.zeros(3 * N, np.float64),
+          "conc": np.zeros(3 * N * m.nsol, np.float64), "C": np.zeros(N * m.nsol, np.float64)}
+    msg = ctypes.c_char_p()
+    rc = lib().pf_init_state(ix, iy, iz, m.nsol, m.cutoff, ctypes.byref(s), _ptr(k), _ptr(c), z0, nz,
+                             _ptr(st["ids"]), _ptr(st["phi"]), _ptr(st["phase"]), _ptr(st["conc"]), _ptr(st["C"]),
+                             ctypes.byref(msg))
+    if rc != 0:
+        raise RuntimeError("pf_init_state: " + (msg.value or b"failed").decode())
+    return st
 
 
 def set_threads(n: int) -> None:

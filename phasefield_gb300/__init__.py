@@ -121,6 +121,8 @@ SYMBOLS = {
     "pf_thermo_read": (_I, [ctypes.c_char_p, ctypes.POINTER(PfModel)]),
     "pf_params_at": (_I, [ctypes.POINTER(PfModel), _D, ctypes.POINTER(PfStepParams)]),
     "pf_init_microstructure": (_I, [ctypes.POINTER(PfModel), ctypes.POINTER(PfInitSpec), _D, _P, _P, _P, _P, _P]),
+    "pf_init_microstructure_box": (_I, [ctypes.POINTER(PfModel), ctypes.POINTER(PfInitSpec), _D, _I, _I, _P, _P, _P,
+                                        _P, _P]),
     "pf_create": (_I, [ctypes.POINTER(PfModel), _I, ctypes.POINTER(_P)]),
     "pf_destroy": (_I, [_P]),
     "pf_set_stream": (_I, [_P, _P]),
@@ -226,6 +228,18 @@ def init_microstructure(model: PfModel, spec: PfInitSpec, time: float) -> dict:
     check(lib().pf_init_microstructure(ctypes.byref(model), ctypes.byref(spec), time, _ptr(st["ids"]),
                                        _ptr(st["phi"]), _ptr(st["phase"]), _ptr(st["conc"]), _ptr(st["C"])),
           "pf_init_microstructure")
+    return st
+
+
+def init_microstructure_box(model: PfModel, spec: PfInitSpec, time: float, z0: int, nz: int) -> dict:
+    """Planes [z0, z0+nz) of the seeded initial state (equal to those planes of
+    init_microstructure on the whole grid)."""
+    N = model.ix * model.iy * nz
+    st = {"ids": np.zeros(6 * N, np.int32), "phi": np.zeros(6 * N, np.float64), "phase": np.zeros(3 * N, np.float64),
+          "conc": np.zeros(3 * N * model.nsol, np.float64), "C": np.zeros(N * model.nsol, np.float64)}
+    check(lib().pf_init_microstructure_box(ctypes.byref(model), ctypes.byref(spec), time, z0, nz, _ptr(st["ids"]),
+                                           _ptr(st["phi"]), _ptr(st["phase"]), _ptr(st["conc"]), _ptr(st["C"])),
+          "pf_init_microstructure_box")
     return st
 
 

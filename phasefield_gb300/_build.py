@@ -57,8 +57,8 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
 
 CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_batch.cu", "pf_reduce.cu", "pf_api.cu",
               "pf_reduce_noalloc.cu", "pf_adjoint.cu"]
-CXX_SOURCES = ["pf_host.cpp"]
-HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h"]
+CXX_SOURCES = ["pf_host.cpp", "pf_init.cpp"]
+HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h", "pf_init.h"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

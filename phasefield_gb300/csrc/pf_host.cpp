@@ -1,6 +1,5 @@
 // pf_host.cpp -- host side of libpfstep: configuration and thermodynamic file
-// parsers, per-step parameter evaluation, the seeded initial microstructure and
-// the reference output writers.
+// parsers, per-step parameter evaluation and the reference output writers.
 //
 // Compiled with -ffp-contract=off: the per-step parameters must come out
 // bit-identical to the reference's host arithmetic (no fused multiply-add).
@@ -17,6 +16,7 @@
 #include <omp.h>
 #endif
 #include "pf_host.h"
+#include "pf_init.h"
 
 namespace {
 thread_local std::string g_last_error;
@@ -412,227 +412,24 @@ extern "C" int pf_write_vti(const char *path, int ix, int iy, int iz, double dx,
 }
 
 // ---------------------------------------------------------------------------
-// Seeded initial microstructure.
+// Seeded initial microstructure: the generator lives in pf_init.cpp (shared
+// with the CPU baseline); here the partition at the start time is evaluated.
 // ---------------------------------------------------------------------------
-namespace {
-
-inline uint64_t splitmix64(uint64_t &s) {
-    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-inline double u01(uint64_t &s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
-// Counter-based uniform for per-cell noise: independent of thread count.
-inline double u01_at(uint64_t seed, uint64_t stream, uint64_t n) {
-    uint64_t s = seed ^ (stream * 0xD1B54A32D192ED03ull) ^ (n * 0x9E3779B97F4A7C15ull);
-    splitmix64(s);
-    return u01(s);
-}
-// Minimum-image separation along one periodic axis (|d| < len on entry).
-inline double mi(double d, int len) {
-    const double L = (double)len;
-    if (d > 0.5 * L) d -= L;
-    else if (d < -0.5 * L) d += L;
-    return d;
-}
-
-struct Cand {
-    int id;
-    double w;
-};
-
-// Periodic bucket grid over sphere centres with bucket edge >= range, so a
-// cell only needs its own and the adjacent buckets.
-struct Buckets {
-    int n[3] = {1, 1, 1};
-    double edge[3] = {1, 1, 1};
-    std::vector<std::vector<int>> items;
-    void build(const std::vector<double> &x, const std::vector<double> &y, const std::vector<double> &z,
-               const int len[3], double range) {
-        for (int d = 0; d < 3; d++) {
-            n[d] = std::max(1, (int)std::floor(len[d] / std::max(range, 1.0)));
-            edge[d] = (double)len[d] / n[d];
-        }
-        items.assign((size_t)n[0] * n[1] * n[2], {});
-        for (size_t g = 0; g < x.size(); g++) {
-            int b[3] = {std::min(n[0] - 1, (int)(x[g] / edge[0])), std::min(n[1] - 1, (int)(y[g] / edge[1])),
-                        std::min(n[2] - 1, (int)(z[g] / edge[2]))};
-            items[b[0] + (size_t)n[0] * (b[1] + (size_t)n[1] * b[2])].push_back((int)g);
-        }
-    }
-    // Candidate indices near point p, ascending (application order is the index order).
-    void near(const double p[3], std::vector<int> &out) const {
-        out.clear();
-        int lists[3][3], cnt[3];
-        for (int d = 0; d < 3; d++) {
-            const int c = std::min(n[d] - 1, (int)(p[d] / edge[d]));
-            if (n[d] >= 3) {
-                lists[d][0] = (c + n[d] - 1) % n[d]; lists[d][1] = c; lists[d][2] = (c + 1) % n[d];
-                cnt[d] = 3;
-            } else {
-                for (int t = 0; t < n[d]; t++) lists[d][t] = t;
-                cnt[d] = n[d];
-            }
-        }
-        for (int a = 0; a < cnt[0]; a++)
-            for (int b = 0; b < cnt[1]; b++)
-                for (int c = 0; c < cnt[2]; c++) {
-                    const auto &v = items[lists[0][a] + (size_t)n[0] * (lists[1][b] + (size_t)n[1] * lists[2][c])];
-                    out.insert(out.end(), v.begin(), v.end());
-                }
-        std::sort(out.begin(), out.end());
-    }
-};
-
-}  // namespace
-
 extern "C" int pf_init_microstructure(const pf_model *model, const pf_init_spec *spec, double time,
                                       int32_t *ids, double *phi, double *phase, double *conc, double *C) {
     if (!model || !spec || !ids || !phi || !phase || !C) return pf_fail(PF_ERR_ARG, "pf_init_microstructure: null argument");
-    const pf_model &m = *model;
-    const int ix = m.ix, iy = m.iy, iz = m.iz;
-    const long long N = (long long)ix * iy * iz;
-    const int K = spec->max_slots < 1 ? 1 : (spec->max_slots > 6 ? 6 : spec->max_slots);
-    if (spec->n_grains < 1) return pf_fail(PF_ERR_ARG, "pf_init_microstructure: need at least one grain");
-    if (spec->n_grains >= PF_MAXGRAIN_PER_PHASE || spec->n_nuclei >= PF_MAXGRAIN_PER_PHASE ||
-        spec->n_particles >= PF_MAXGRAIN_PER_PHASE)
-        return pf_fail(PF_ERR_RANGE, "pf_init_microstructure: too many grains");
-    const double W = spec->width > 0 ? spec->width : 6.0;
-    const double kk = 3.0 / W;  // tanh(3*h/W): 5%..95% over one interface width
-    uint64_t s = spec->seed;
-    std::vector<double> gx(spec->n_grains), gy(spec->n_grains), gz(spec->n_grains);
-    for (int g = 0; g < spec->n_grains; g++) {
-        gx[g] = u01(s) * ix; gy[g] = u01(s) * iy; gz[g] = u01(s) * iz;
-    }
-    std::vector<double> nx(spec->n_nuclei), ny(spec->n_nuclei), nz(spec->n_nuclei);
-    for (int g = 0; g < spec->n_nuclei; g++) {
-        nx[g] = u01(s) * ix; ny[g] = u01(s) * iy; nz[g] = u01(s) * iz;
-    }
-    std::vector<double> px(spec->n_particles), py(spec->n_particles), pz(spec->n_particles);
-    for (int g = 0; g < spec->n_particles; g++) {
-        px[g] = u01(s) * ix; py[g] = u01(s) * iy; pz[g] = u01(s) * iz;
-    }
-    pf_step_params P;
-    pf_compute_params(m, time, P);
-    const uint64_t seed = spec->seed;
-    const bool zflat = (iz == 1), yflat = (iy == 1);
-    const long long nsol = m.nsol;
-    const int len[3] = {ix, iy, iz};
-    Buckets bnuc, bpar;
-    bnuc.build(nx, ny, nz, len, spec->nucleus_radius + 3.0 / kk + 1.0);
-    bpar.build(px, py, pz, len, spec->particle_radius + 3.0 / kk + 1.0);
+    return pf_init_microstructure_box(model, spec, time, 0, model->iz, ids, phi, phase, conc, C);
+}
 
-#pragma omp parallel
-    {
-    std::vector<int> near;
-    near.reserve(256);
-#pragma omp for schedule(dynamic, 256)
-    for (long long n = 0; n < N; n++) {
-        const int i = (int)(n % ix);
-        const int j = (int)((n / ix) % iy);
-        const int k = (int)(n / ((long long)ix * iy));
-        const double x = i, y = j, z = k;
-        // Ferrite matrix: periodic Voronoi with a tanh profile across each
-        // bisector.  Keep the few nearest seeds.
-        constexpr int KN = 6;
-        int best[KN];
-        double bd2[KN], bvx[KN], bvy[KN], bvz[KN];
-        int nb = 0;
-        for (int g = 0; g < spec->n_grains; g++) {
-            const double vx = mi(gx[g] - x, ix), vy = yflat ? 0 : mi(gy[g] - y, iy), vz = zflat ? 0 : mi(gz[g] - z, iz);
-            const double d2 = vx * vx + vy * vy + vz * vz;
-            if (nb < KN || d2 < bd2[nb - 1]) {
-                int pos = nb < KN ? nb++ : KN - 1;
-                while (pos > 0 && bd2[pos - 1] > d2) {
-                    best[pos] = best[pos - 1]; bd2[pos] = bd2[pos - 1];
-                    bvx[pos] = bvx[pos - 1]; bvy[pos] = bvy[pos - 1]; bvz[pos] = bvz[pos - 1];
-                    pos--;
-                }
-                best[pos] = g; bd2[pos] = d2; bvx[pos] = vx; bvy[pos] = vy; bvz[pos] = vz;
-            }
-        }
-        // Signed distance to each candidate's Voronoi cell boundary facing the
-        // nearest seed: h_g = (|b|^2 - |a|^2) / (2|b - a|) for g != nearest,
-        // and the nearest grain's depth -min_g h_g.
-        Cand cand[16];
-        int nc = 0;
-        double hmin = 1e30;
-        double hg[KN];
-        for (int t = 1; t < nb; t++) {
-            const double dx_ = bvx[t] - bvx[0], dy_ = bvy[t] - bvy[0], dz_ = bvz[t] - bvz[0];
-            const double sep = std::sqrt(dx_ * dx_ + dy_ * dy_ + dz_ * dz_);
-            hg[t] = sep > 0 ? (bd2[t] - bd2[0]) / (2 * sep) : 0.0;
-            if (hg[t] < hmin) hmin = hg[t];
-        }
-        hg[0] = nb > 1 ? -hmin : -1e30;
-        double wsum = 0;
-        for (int t = 0; t < nb; t++) {
-            const double a = kk * hg[t];
-            const double w = a >= 3.0 ? 0.0 : (a <= -3.0 ? 1.0 : 0.5 * (1.0 - std::tanh(a)));
-            if (w > 0) { cand[nc++] = {100000 + best[t] + 1, w}; wsum += w; }
-        }
-        for (int t = 0; t < nc; t++) cand[t].w /= wsum;
-        // Nuclei and particles: spheres (discs in 2D) with the same profile.
-        auto add_spheres = [&](const std::vector<double> &sx, const std::vector<double> &sy,
-                               const std::vector<double> &sz, double r, int base, const Buckets &bk) {
-            const double p[3] = {x, y, z};
-            bk.near(p, near);
-            for (int g : near) {
-                const double vx = mi(sx[g] - x, ix), vy = yflat ? 0 : mi(sy[g] - y, iy), vz = zflat ? 0 : mi(sz[g] - z, iz);
-                const double a = kk * (std::sqrt(vx * vx + vy * vy + vz * vz) - r);
-                if (a >= 3.0) continue;
-                const double w = a <= -3.0 ? 1.0 : 0.5 * (1.0 - std::tanh(a));
-                // Insert w for this inclusion, scaling what was there by (1-w).
-                double keep = 1.0 - w;
-                for (int t = 0; t < nc; t++) cand[t].w *= keep;
-                if (nc < 16) cand[nc++] = {base + (int)g + 1, w};
-                else {
-                    int lo = 0;
-                    for (int t = 1; t < nc; t++) if (cand[t].w < cand[lo].w) lo = t;
-                    if (cand[lo].w < w) cand[lo] = {base + (int)g + 1, w};
-                }
-            }
-        };
-        add_spheres(nx, ny, nz, spec->nucleus_radius, 200000, bnuc);
-        add_spheres(px, py, pz, spec->particle_radius, 300000, bpar);
-        // Largest K with weight above the cutoff, sorted descending, renormalised.
-        for (int a = 0; a < nc; a++)
-            for (int b = a + 1; b < nc; b++)
-                if (cand[b].w > cand[a].w) std::swap(cand[a], cand[b]);
-        int keep = 0;
-        double sum = 0;
-        for (int a = 0; a < nc && keep < K; a++)
-            if (cand[a].w > 10.0 * m.cutoff) { keep++; sum += cand[a].w; }
-        double ph[3] = {0, 0, 0};
-        for (int a = 0; a < 6; a++) {
-            if (a < keep) {
-                const double v = cand[a].w / sum;
-                ids[6 * n + a] = cand[a].id;
-                phi[6 * n + a] = v;
-                ph[cand[a].id / PF_MAXGRAIN_PER_PHASE - 1] += v;
-            } else {
-                ids[6 * n + a] = 0;
-                phi[6 * n + a] = 0.0;
-            }
-        }
-        for (int p = 0; p < 3; p++) phase[3 * n + p] = ph[p];
-        for (long long q = 0; q < nsol; q++) {
-            const double c = spec->C0[q] + spec->C_noise[q] * (2.0 * u01_at(seed, 1 + q, (uint64_t)n) - 1.0);
-            C[q * N + n] = c;
-            if (conc) {
-                // solver.cpp:389-405
-                for (int a = 1; a <= 3; a++) {
-                    double t1 = 0., t2 = 0.;
-                    for (int b = 1; b <= 3; b++) {
-                        t1 += ph[b - 1] * P.k[q][e3(a, b)];
-                        t2 += ph[b - 1] * P.c[q][e3(a, b)];
-                    }
-                    conc[q * 3 * N + 3 * n + a - 1] = (c - t2) / t1;
-                }
-            }
-        }
-    }
-    }  // omp parallel
-    return PF_OK;
+extern "C" int pf_init_microstructure_box(const pf_model *model, const pf_init_spec *spec, double time, int z0,
+                                          int nz, int32_t *ids, double *phi, double *phase, double *conc,
+                                          double *C) {
+    if (!model || !spec || !ids || !phi || !phase || !C)
+        return pf_fail(PF_ERR_ARG, "pf_init_microstructure_box: null argument");
+    pf_step_params P;
+    pf_compute_params(*model, time, P);
+    const char *msg = nullptr;
+    const int st = pf_init_state(model->ix, model->iy, model->iz, model->nsol, model->cutoff, spec, &P.k[0][0],
+                                 &P.c[0][0], z0, nz, ids, phi, phase, conc, C, &msg);
+    return st == PF_OK ? PF_OK : pf_fail(st, std::string("pf_init_microstructure: ") + (msg ? msg : "failed"));
 }

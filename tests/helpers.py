@@ -47,3 +47,29 @@ def rel_maxnorm(a: np.ndarray, b: np.ndarray) -> float:
     """max|a-b| / max(max|b|, tiny): the relative max-norm used for parity."""
     scale = max(float(np.max(np.abs(b))), 1e-300)
     return float(np.max(np.abs(a - b))) / scale
+
+
+REF_CPU_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cpu_steps.npz")
+REF_CPU_CASES = ("2d", "ragged6", "3d", "cem", "line")
+
+
+def ref_cpu_case(tmpdir: str, golden, name: str):
+    """One case of tests/golden/ref_cpu_steps.npz (outputs of the reference's own
+    CPU code): writes its configuration (output folder moved under tmpdir) and
+    thermodynamic file, and returns (config path, initial state, expected)."""
+    os.makedirs(tmpdir, exist_ok=True)
+    lines = str(golden[f"{name}_config"]).splitlines()
+    lines[1] = os.path.join(tmpdir, "out")
+    os.makedirs(lines[1], exist_ok=True)
+    cfg = os.path.join(tmpdir, f"{name}.txt")
+    with open(cfg, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    with open(os.path.join(tmpdir, "thermo_steel.txt"), "w") as f:
+        f.write(str(golden[f"{name}_thermo"]))
+    st0 = {k: golden[f"{name}_{k}0"].copy() for k in ("ids", "phi", "phase", "conc", "C")}
+    exp = {k: golden[f"{name}_{k}"] for k in ("ids", "phi", "phase", "conc", "C")}
+    exp["time"] = float(golden[f"{name}_time"])
+    exp["steps"] = int(golden[f"{name}_steps"])
+    exp["fraction"] = str(golden[f"{name}_fraction"])
+    exp["vti"] = str(golden[f"{name}_vti"]) if f"{name}_vti" in golden.files else None
+    return cfg, st0, exp
