@@ -324,7 +324,7 @@ def run_precision(args) -> dict:
         return out
 
     def err(a32, ref_phase, ref_C, N):
-        d = np.abs(a32["phase"] - ref_phase)
+        d = np.abs(a32["phase"][:3 * N] - ref_phase)
         fr32 = a32["phase"].reshape(N, 3).mean(0)
         frr = ref_phase.reshape(N, 3).mean(0)
         return {"phase_max_abs": float(d.max()), "phase_mean_abs": float(d.mean()),
@@ -345,6 +345,32 @@ def run_precision(args) -> dict:
     out = {"grid": [args.precision_grid] * 3, "steps": S, "cells": N,
            "vs_fp64_four_slot": err(a32, a4["phase"], a4["C"], N),
            "carbon_mass_rel_drift_fp32": float(abs(a32["reduce"][4] - C0) / C0)}
+    if args.sensitivity_grid > 0:
+        # How far the FP64 four-slot model itself moves when only its input is
+        # rounded: phi rounded to FP32 (what the compact layout stores), or
+        # perturbed by a few FP64 ulps.  Pointwise differences of this size are
+        # a property of the model's discrete decisions (clamps at 0 / 1 and the
+        # cutoff, top-four choice), not of the arithmetic precision.
+        ms, sts, Ns = setup(args.sensitivity_grid)
+
+        def fp64_four_slot(state):
+            A = pf.Adjoint(ms, pf.PF_PREC_FP64, max(S, 1))
+            A.upload(state, 0.0)
+            A.forward(S)
+            out = A.final_state()
+            A.close()
+            return out
+
+        base = fp64_four_slot(sts)
+        r32 = dict(sts, phi=sts["phi"].astype(np.float32).astype(np.float64))
+        ulp = dict(sts, phi=sts["phi"] * (1.0 + 4.0 * np.finfo(np.float64).eps))
+        c32 = fp32(ms, sts)
+        out["sensitivity_fp64_four_slot"] = {
+            "grid": [args.sensitivity_grid] * 3,
+            "fp64_input_rounded_to_fp32": err(fp64_four_slot(r32), base["phase"], base["C"], Ns),
+            "fp64_input_times_1p4ulp": err(fp64_four_slot(ulp), base["phase"], base["C"], Ns),
+            "fp32c": err(c32, base["phase"], base["C"], Ns),
+        }
     if args.six_slot_grid > 0:
         m6, st6, N6 = setup(args.six_slot_grid)
         b32 = fp32(m6, st6)
@@ -567,6 +593,8 @@ def main() -> None:
     ap.add_argument("--adjoint-steps", type=int, default=2000, help="steps of the adjoint calibration run (0 = skip)")
     ap.add_argument("--precision-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 error run (0 = skip)")
     ap.add_argument("--precision-grid", type=int, default=256, help="cube side of the FP32-vs-FP64 error run")
+    ap.add_argument("--sensitivity-grid", type=int, default=128,
+                    help="cube side of the FP64 self-sensitivity comparison (0 = skip)")
     ap.add_argument("--six-slot-grid", type=int, default=128,
                     help="cube side of the FP32C-vs-six-slot-FP64 comparison (0 = skip)")
     ap.add_argument("--grid", type=int, nargs=3, default=None, help="override the workload grid")

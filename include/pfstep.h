@@ -196,6 +196,8 @@ int pf_reduce(pf_ctx *ctx, double out[8]);
  * reference_totals is NULL or max_rel_drift <= 0).  out (may be NULL) receives
  * the pf_reduce statistics. */
 int pf_check_state(pf_ctx *ctx, const double reference_totals[2], double max_rel_drift, double out[8]);
+/* Waits for the context's stream; PF_ERR_TIMEOUT if a bounded device-side
+ * wait of the staged diffusion kernel ran out since the last check. */
 int pf_synchronize(pf_ctx *ctx);
 int pf_get_time(pf_ctx *ctx, double *time);
 int pf_last_params(pf_ctx *ctx, pf_step_params *out);
@@ -209,11 +211,14 @@ int pf_kernel_times(pf_ctx *ctx, double times_ms[2], long long counts[2]);
 int pf_use_graph(pf_ctx *ctx, int on);
 /* Time every candidate tile shape of the FP32C diffusion kernel on the
  * context's own state and keep the fastest (state unchanged); reports the
- * chosen tile height, z chunk, kernel variant (always 0: one sub-step per
- * pass over the grid) and mean launch time.  No-op for FP64. */
+ * chosen tile height, z chunk, kernel variant (0: plain loads one plane
+ * ahead; 1: tile interior staged by TMA, 3D tile-aligned grids only -- both
+ * give identical results) and mean launch time.  No-op for FP64. */
 int pf_autotune(pf_ctx *ctx, int *tile_y, int *zchunk, int *variant, float *ms);
-/* Fix the FP32C diffusion tile shape (tile_y 4/8/16, z chunk >= 1, variant
- * 0; anything else is PF_ERR_ARG); tile_y = 0 returns to the default rule. */
+/* Fix the FP32C diffusion tile shape: tile_y 8/16/32 rows of a 64-cell-wide
+ * tile with variant 0, or 8/16 with variant 1 on a 3D grid whose x extent is a
+ * multiple of 64 and y extent a multiple of tile_y; z chunk >= 1; anything
+ * else is PF_ERR_ARG.  tile_y = 0 returns to the default rule. */
 int pf_set_diffusion_tile(pf_ctx *ctx, int tile_y, int zchunk, int variant);
 /* The autotuner's candidates as (tile_y, zchunk, variant) triples; returns
  * how many were written (at most max). */

@@ -624,8 +624,14 @@ extern "C" int pf_set_diffusion_tile(pf_ctx *c, int ty, int zchunk, int variant)
         c->diff_cfg_valid = false;
         return PF_OK;
     }
-    if ((ty != 4 && ty != 8 && ty != 16) || zchunk < 1 || variant != 0)
-        return pf_fail(PF_ERR_ARG, "pf_set_diffusion_tile: tile height 4/8/16, z chunk >= 1, variant 0");
+    pf_step_params P;
+    pf_compute_params(c->model, c->time, P);
+    pf_f32_params F;
+    pf_fold_f32(P, c->map.off[2], c->map.off[3], F);
+    if (zchunk < 1 || !pf_diffuse_variant_ok(F, ty, variant))
+        return pf_fail(PF_ERR_ARG,
+                       "pf_set_diffusion_tile: tile height 8/16/32 with variant 0, or 8/16 with variant 1 on a 3D grid "
+                       "whose x extent is a multiple of 64 and y extent a multiple of the tile height; z chunk >= 1");
     c->diff_cfg = pf_diff_cfg{ty, zchunk, variant};
     c->diff_cfg_valid = true;
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
@@ -686,6 +692,8 @@ extern "C" int pf_check_state(pf_ctx *c, const double reference_totals[2], doubl
 extern "C" int pf_synchronize(pf_ctx *c) {
     if (!c) return pf_fail(PF_ERR_ARG, "pf_synchronize: null context");
     PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    if (pf_diffuse_take_timeout())
+        return pf_fail(PF_ERR_TIMEOUT, "pf_synchronize: a bounded wait of the staged diffusion kernel ran out");
     return PF_OK;
 }
 

@@ -37,10 +37,14 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
 struct pf_diff_cfg {
     int ty;
     int zchunk;
-    int variant; // 0: one sub-step per pass over the grid
+    int variant; // 0: plain loads one plane ahead; 1: tile interior staged by TMA (same results)
 };
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P);
 int pf_diffuse_candidates(const pf_f32_params &P, pf_diff_cfg *out, int max);
+// Whether (tile height, variant) can run on this grid.
+bool pf_diffuse_variant_ok(const pf_f32_params &P, int ty, int variant);
+// 1 if a bounded wait of the TMA variant ran out since the last call (then cleared).
+int pf_diffuse_take_timeout();
 // 'sphase' holds the square roots of the phase fractions (pf_f32.cuh).
 cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, const float2 *sol_in,
                                   float2 *sol_out, cudaStream_t s, const pf_diff_cfg *cfg);
