@@ -243,6 +243,12 @@ int pf_batch_info(pf_batch *b, long long out[4]);
 /* Barrier wait limit; unreachable_barrier != 0 makes every group barrier wait
  * for one block too many (to exercise the timeout path in tests). */
 int pf_batch_set_timeout(pf_batch *b, unsigned long long timeout_ns, int unreachable_barrier);
+/* Tile shape of the persistent kernel: 32 x tile_y cells (tile_y 4 or 8), using
+ * 1/occupancy_divisor (1..4) of the resident-block capacity. */
+int pf_batch_set_tile(pf_batch *b, int tile_y, int occupancy_divisor);
+/* Time every tile shape on nsteps of the current ensemble (the states are
+ * restored afterwards) and keep the fastest; reports it and its time. */
+int pf_batch_autotune(pf_batch *b, int nsteps, int *tile_y, int *occupancy_divisor, float *ms);
 int pf_batch_destroy(pf_batch *b);
 
 /* Adjoint of the explicit step (no reference counterpart), for calibration.

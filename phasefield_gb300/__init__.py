@@ -153,6 +153,8 @@ SYMBOLS = {
     "pf_batch_reduce": (_I, [_P, _I, _DP]),
     "pf_batch_info": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     "pf_batch_set_timeout": (_I, [_P, ctypes.c_ulonglong, _I]),
+    "pf_batch_set_tile": (_I, [_P, _I, _I]),
+    "pf_batch_autotune": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float)]),
     "pf_batch_destroy": (_I, [_P]),
     "pf_adj_create": (_I, [ctypes.POINTER(PfModel), _I, _I, ctypes.POINTER(_P)]),
     "pf_adj_upload": (_I, [_P, _P, _P, _P, _P, _D]),
@@ -435,6 +437,16 @@ class Batch:
 
     def set_timeout(self, timeout_ns: int, unreachable_barrier: bool = False) -> None:
         check(lib().pf_batch_set_timeout(self._b, timeout_ns, int(unreachable_barrier)), "pf_batch_set_timeout")
+
+    def set_tile(self, tile_y: int, occupancy_divisor: int = 1) -> None:
+        check(lib().pf_batch_set_tile(self._b, tile_y, occupancy_divisor), "pf_batch_set_tile")
+
+    def autotune(self, nsteps: int) -> dict:
+        """Pick the persistent kernel's tile shape by timing each on nsteps (states restored)."""
+        ty, dv, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        check(lib().pf_batch_autotune(self._b, nsteps, ctypes.byref(ty), ctypes.byref(dv), ctypes.byref(ms)),
+              "pf_batch_autotune")
+        return {"tile_y": ty.value, "occupancy_divisor": dv.value, "ms": ms.value}
 
 
 class Adjoint:

@@ -757,7 +757,11 @@ struct pf_batch {
     unsigned long long timeout_ns = 2000000000ull;  // 2 s per barrier wait
     int extra_target = 0;
     cudaGraphExec_t gexec = nullptr;
-    int g_steps = -1, g_blocks = -1;
+    int g_steps = -1, g_blocks = -1, g_tile = -1;
+    // Tile height of the persistent kernel and the fraction (1/occ_div) of
+    // the resident-block capacity it uses: chosen by pf_batch_autotune.
+    int tile_y = 8, occ_div = 1;
+    int sms = 0;
 };
 
 namespace {
@@ -798,8 +802,11 @@ extern "C" int pf_batch_create(const pf_model *models, int ndom, pf_batch **out)
     if (st == PF_OK) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        b->max_blocks = pf_batch_blocks_per_sm(b->nsol) * sms;
-        if (b->max_blocks < ndom) st = pf_fail(PF_ERR_RANGE, "pf_batch_create: more domains than resident blocks");
+        b->sms = sms;
+        // Capacity for the largest candidate launch (4-row tiles, full occupancy).
+        b->max_blocks = pf_batch_blocks_per_sm(b->nsol, 4) * sms;
+        if (pf_batch_blocks_per_sm(b->nsol, 8) * sms < ndom)
+            st = pf_fail(PF_ERR_RANGE, "pf_batch_create: more domains than resident blocks");
     }
     bool ok = st == PF_OK;
     auto dalloc = [&](void **p, size_t n) { if (ok && cudaMalloc(p, n) != cudaSuccess) ok = false; };
@@ -891,7 +898,9 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
         if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_batch_run: a domain has no state");
     if (nsteps == 0) return PF_OK;
     // Parameters, and block groups sized by work (phase sweep ~ 2 sub-steps).
-    const int tile = pf_batch_tile_cells();
+    const int ty_tile = b->tile_y;
+    const int cap = pf_batch_blocks_per_sm(b->nsol, ty_tile) * b->sms / b->occ_div;
+    if (cap < nd) return pf_fail(PF_ERR_RANGE, "pf_batch_run: more domains than resident blocks for this tile shape");
     std::vector<double> w(nd);
     std::vector<int> tiles(nd), nsub(nd);
     double wsum = 0.;
@@ -901,23 +910,22 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
         pf_compute_params(c->model, c->time, P);
         pf_fold_f32(P, c->map.off[2], c->map.off[3], b->h_params[d]);
         nsub[d] = P.n_sub;
-        const int tx = (c->model.ix + 31) / 32, ty = (c->model.iy + 7) / 8;
+        const int tx = (c->model.ix + 31) / 32, ty = (c->model.iy + ty_tile - 1) / ty_tile;
         tiles[d] = tx * ty;
         w[d] = (double)c->N * (2 + P.n_sub);
         wsum += w[d];
         b->h_doms[d].tiles_x = tx;
         b->h_doms[d].tiles = tiles[d];
     }
-    (void)tile;
     std::vector<int> nb(nd);
     int used = 0;
     for (int d = 0; d < nd; d++) {
-        nb[d] = (int)((double)b->max_blocks * w[d] / wsum);
+        nb[d] = (int)((double)cap * w[d] / wsum);
         if (nb[d] < 1) nb[d] = 1;
         if (nb[d] > tiles[d]) nb[d] = tiles[d];
         used += nb[d];
     }
-    while (used > b->max_blocks) {  // trim the largest groups
+    while (used > cap) {  // trim the largest groups
         int big = 0;
         for (int d = 1; d < nd; d++)
             if (nb[d] > nb[big]) big = d;
@@ -942,7 +950,7 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
     b->nblocks = used;
     // One graph per (steps, block count): the memcpy nodes read the pinned
     // host tables at replay, so updated buffer roles and parameters flow in.
-    if (!b->gexec || b->g_steps != nsteps || b->g_blocks != used) {
+    if (!b->gexec || b->g_steps != nsteps || b->g_blocks != used || b->g_tile != ty_tile) {
         if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
         cudaGraph_t g;
         PF_CUDA_OK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -951,8 +959,8 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
         cudaMemcpyAsync(b->d_block_dom, b->h_block_dom, sizeof(int) * used, cudaMemcpyHostToDevice, b->stream);
         cudaMemsetAsync(b->d_ctr, 0, sizeof(unsigned long long) * nd, b->stream);
         cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
-        cudaError_t e1 = pf_launch_batch(b->nsol, used, b->d_doms, b->d_params, b->d_block_dom, nsteps, b->d_ctr,
-                                         b->d_err, b->timeout_ns, b->stream);
+        cudaError_t e1 = pf_launch_batch(b->nsol, ty_tile, used, b->d_doms, b->d_params, b->d_block_dom, nsteps,
+                                         b->d_ctr, b->d_err, b->timeout_ns, b->stream);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess) return pf_cuda_fail(e1 != cudaSuccess ? e1 : e2);
         cudaError_t e3 = cudaGraphInstantiate(&b->gexec, g, 0);
@@ -960,6 +968,7 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
         if (e3 != cudaSuccess) return pf_cuda_fail(e3);
         b->g_steps = nsteps;
         b->g_blocks = used;
+        b->g_tile = ty_tile;
     }
     PF_CUDA_OK(cudaGraphLaunch(b->gexec, b->stream));
     PF_CUDA_OK(cudaMemcpyAsync(b->h_err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
@@ -977,6 +986,105 @@ extern "C" int pf_batch_run(pf_batch *b, int nsteps) {
         c->last = P;
         c->have_last = true;
     }
+    return PF_OK;
+}
+
+extern "C" int pf_batch_set_tile(pf_batch *b, int tile_y, int occupancy_divisor) {
+    if (!b || !pf_batch_tile_ok(tile_y) || occupancy_divisor < 1 || occupancy_divisor > 4)
+        return pf_fail(PF_ERR_ARG, "pf_batch_set_tile: tile height 4 or 8, occupancy divisor 1..4");
+    b->tile_y = tile_y;
+    b->occ_div = occupancy_divisor;
+    return PF_OK;
+}
+
+// Autotuner of the persistent kernel's shape: each candidate (tile height x
+// fraction of the resident-block capacity) advances every domain nsteps from
+// the current states -- once to build its graph, once timed -- and the states
+// are restored after every trial, so the ensemble is left exactly as it was.
+extern "C" int pf_batch_autotune(pf_batch *b, int nsteps, int *tile_y, int *occupancy_divisor, float *ms) {
+    if (!b || nsteps < 1) return pf_fail(PF_ERR_ARG, "pf_batch_autotune: bad arguments");
+    struct Snap {
+        void *buf[7];
+        size_t bytes[7];
+        int cur, curs;
+        double time;
+        pf_step_params last;
+        bool have_last;
+    };
+    std::vector<Snap> snap(b->dom.size());
+    int st = PF_OK;
+    for (size_t d = 0; d < b->dom.size() && st == PF_OK; d++) {
+        pf_ctx *c = b->dom[d];
+        if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_batch_autotune: a domain has no state");
+        const size_t N = (size_t)c->N;
+        void *src[7] = {c->gid[0], c->gid[1], c->phi32[0], c->phi32[1], c->phase32, c->sol[0], c->sol[1]};
+        const size_t by[7] = {N * sizeof(ushort4), N * sizeof(ushort4), N * sizeof(float4), N * sizeof(float4),
+                              3 * N * sizeof(float), N * c->nsol * sizeof(float2), N * c->nsol * sizeof(float2)};
+        Snap &S = snap[d];
+        for (int k = 0; k < 7; k++) {
+            S.buf[k] = nullptr;
+            S.bytes[k] = by[k];
+            if (st == PF_OK && cudaMalloc(&S.buf[k], by[k]) != cudaSuccess) {
+                cudaGetLastError();
+                st = pf_fail(PF_ERR_NOMEM, "pf_batch_autotune: snapshot allocation failed");
+            }
+            if (st == PF_OK) cudaMemcpyAsync(S.buf[k], src[k], by[k], cudaMemcpyDeviceToDevice, b->stream);
+        }
+        S.cur = c->cur; S.curs = c->curs; S.time = c->time; S.last = c->last; S.have_last = c->have_last;
+    }
+    auto restore = [&]() {
+        for (size_t d = 0; d < b->dom.size(); d++) {
+            pf_ctx *c = b->dom[d];
+            void *dst[7] = {c->gid[0], c->gid[1], c->phi32[0], c->phi32[1], c->phase32, c->sol[0], c->sol[1]};
+            const Snap &S = snap[d];
+            for (int k = 0; k < 7; k++) cudaMemcpyAsync(dst[k], S.buf[k], S.bytes[k], cudaMemcpyDeviceToDevice, b->stream);
+            c->cur = S.cur; c->curs = S.curs; c->time = S.time; c->last = S.last; c->have_last = S.have_last;
+        }
+    };
+    const int old_ty = b->tile_y, old_div = b->occ_div;
+    int best_ty = old_ty, best_div = old_div;
+    float best = 1e30f;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st == PF_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        st = pf_fail(PF_ERR_CUDA, "pf_batch_autotune: event creation failed");
+    const int tys[2] = {4, 8}, divs[2] = {1, 2};
+    for (int a = 0; a < 2 && st == PF_OK; a++)
+        for (int v = 0; v < 2 && st == PF_OK; v++) {
+            b->tile_y = tys[a];
+            b->occ_div = divs[v];
+            if (pf_batch_blocks_per_sm(b->nsol, tys[a]) * b->sms / divs[v] < (int)b->dom.size()) continue;
+            restore();
+            st = pf_batch_run(b, nsteps);  // builds this shape's graph
+            if (st != PF_OK) break;
+            restore();
+            cudaEventRecord(e0, b->stream);
+            st = pf_batch_run(b, nsteps);
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (st == PF_OK && t < best) {
+                best = t;
+                best_ty = tys[a];
+                best_div = divs[v];
+            }
+        }
+    if (!snap.empty() && snap[0].buf[0]) restore();
+    cudaStreamSynchronize(b->stream);
+    for (auto &S : snap)
+        for (int k = 0; k < 7; k++) cudaFree(S.buf[k]);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st != PF_OK) {
+        b->tile_y = old_ty;
+        b->occ_div = old_div;
+        return st;
+    }
+    b->tile_y = best_ty;
+    b->occ_div = best_div;
+    if (tile_y) *tile_y = best_ty;
+    if (occupancy_divisor) *occupancy_divisor = best_div;
+    if (ms) *ms = best;
     return PF_OK;
 }
 

@@ -19,7 +19,7 @@
 
 namespace {
 
-constexpr int kBX = 32, kBY = 8, kBT = kBX * kBY;
+constexpr int kBX = 32;  // tile width; the tile height BY (4 or 8) is chosen by pf_batch_autotune
 
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;
@@ -59,9 +59,9 @@ template <int NSOL> struct BVec;
 template <> struct BVec<1> { using T = float2; };
 template <> struct BVec<2> { using T = float4; };
 
-template <int NSOL>
+template <int NSOL, int BY>
 struct BRec {
-    typename BVec<NSOL>::T rec[3][kBY + 2][kBX + 2];
+    typename BVec<NSOL>::T rec[3][BY + 2][kBX + 2];
 };
 
 template <int NSOL>
@@ -78,25 +78,23 @@ __device__ __forceinline__ void load_raw_cg(const float *sph, const float2 *sol,
     }
 }
 
-template <int NSOL>
-__device__ __forceinline__ void store_rec(BRec<NSOL> &R, int y, int x, const float s[3], const float c[NSOL][3]);
-template <>
-__device__ __forceinline__ void store_rec<1>(BRec<1> &R, int y, int x, const float s[3], const float c[1][3]) {
+template <int BY>
+__device__ __forceinline__ void store_rec(BRec<1, BY> &R, int y, int x, const float s[3], const float c[1][3]) {
 #pragma unroll
     for (int p = 0; p < 3; p++) R.rec[p][y][x] = make_float2(s[p], c[0][p]);
 }
-template <>
-__device__ __forceinline__ void store_rec<2>(BRec<2> &R, int y, int x, const float s[3], const float c[2][3]) {
+template <int BY>
+__device__ __forceinline__ void store_rec(BRec<2, BY> &R, int y, int x, const float s[3], const float c[2][3]) {
 #pragma unroll
     for (int p = 0; p < 3; p++) R.rec[p][y][x] = make_float4(s[p], c[0][p], c[1][p], 0.f);
 }
 __device__ __forceinline__ float rec_conc(const float2 &v, int) { return v.y; }
 __device__ __forceinline__ float rec_conc(const float4 &v, int q) { return q == 0 ? v.y : v.z; }
 
-// One 32x8 tile of one diffusion sub-step of a 2D domain.
-template <int NSOL>
+// One 32 x BY tile of one diffusion sub-step of a 2D domain.
+template <int NSOL, int BY>
 __device__ __forceinline__ void diffuse_tile(const pf_f32_params &P, int tx0, int ty0, const float *sph,
-                                             const float2 *sol_in, float2 *sol_out, BRec<NSOL> &R) {
+                                             const float2 *sol_in, float2 *sol_out, BRec<NSOL, BY> &R) {
     const int tid = threadIdx.x;
     const int lx = tid % kBX, ly = tid / kBX;
     const int ix = P.ix, iy = P.iy;
@@ -110,21 +108,22 @@ __device__ __forceinline__ void diffuse_tile(const pf_f32_params &P, int tx0, in
 #pragma unroll
         for (int q = 0; q < NSOL; q++) pf_partition_q(P, q, C[q], ph, c[q]);
     }
-    store_rec<NSOL>(R, ly + 1, lx + 1, s, c);
-    constexpr int NH = 2 * kBX + 2 * kBY;
-    if (tid < NH) {
+    store_rec(R, ly + 1, lx + 1, s, c);
+    // Halo ring: 2*kBX + 2*BY cells, one or two per thread.
+    constexpr int NH = 2 * kBX + 2 * BY, NT = kBX * BY;
+    for (int hid = tid; hid < NH; hid += NT) {
         int hx, hy;
-        if (tid < kBX) { hx = tid; hy = -1; }
-        else if (tid < 2 * kBX) { hx = tid - kBX; hy = kBY; }
-        else if (tid < 2 * kBX + kBY) { hx = -1; hy = tid - 2 * kBX; }
-        else { hx = kBX; hy = tid - 2 * kBX - kBY; }
+        if (hid < kBX) { hx = hid; hy = -1; }
+        else if (hid < 2 * kBX) { hx = hid - kBX; hy = BY; }
+        else if (hid < 2 * kBX + BY) { hx = -1; hy = hid - 2 * kBX; }
+        else { hx = kBX; hy = hid - 2 * kBX - BY; }
         const long long h = pf_mod(tx0 + hx, ix) + (long long)ix * pf_mod(ty0 + hy, iy);
         float hs[3], hC[NSOL], hcomp[NSOL], hc[NSOL][3];
         load_raw_cg<NSOL>(sph, sol_in, N, h, hs, hC, hcomp);
         const float hph[3] = {hs[0] * hs[0], hs[1] * hs[1], hs[2] * hs[2]};
 #pragma unroll
         for (int q = 0; q < NSOL; q++) pf_partition_q(P, q, hC[q], hph, hc[q]);
-        store_rec<NSOL>(R, hy + 1, hx + 1, hs, hc);
+        store_rec(R, hy + 1, hx + 1, hs, hc);
     }
     __syncthreads();
     if (valid) {
@@ -159,14 +158,15 @@ __device__ __forceinline__ void diffuse_tile(const pf_f32_params &P, int tx0, in
     __syncthreads();
 }
 
-template <int NSOL>
-__global__ void __launch_bounds__(kBT, 4) k_batch(const pf_batch_dom *__restrict__ doms,
+template <int NSOL, int BY>
+__global__ void __launch_bounds__(kBX * BY, 1024 / (kBX * BY)) k_batch(const pf_batch_dom *__restrict__ doms,
                                                const pf_f32_params *__restrict__ params,
                                                const int *__restrict__ block_dom, int nsteps,
                                                unsigned long long *ctr, int *err, unsigned long long timeout_ns) {
+    constexpr int kBT = kBX * BY;
     __shared__ union U {
         pf_plist<kBT> L;
-        BRec<NSOL> R;
+        BRec<NSOL, BY> R;
     } sm;
     __shared__ pf_f32_params P;
     const int d = block_dom[blockIdx.x];
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kBT, 4) k_batch(const pf_batch_dom *__restrict
     for (int step = 0; step < nsteps; step++) {
         // Phase sweep of the group's tiles.
         for (int tile = lb; tile < D.tiles; tile += nb) {
-            const int tx0 = (tile % D.tiles_x) * kBX, ty0 = (tile / D.tiles_x) * kBY;
+            const int tx0 = (tile % D.tiles_x) * kBX, ty0 = (tile / D.tiles_x) * BY;
             const int i = tx0 + threadIdx.x % kBX, j = ty0 + threadIdx.x / kBX;
             if (i < P.ix && j < P.iy)
                 pf_phase_cell<NSOL, kBT, true>(P, i, j, 0, threadIdx.x, D.gid[g], D.phi[g], D.gid[g ^ 1],
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kBT, 4) k_batch(const pf_batch_dom *__restrict
         g ^= 1;
         for (int sub = 0; sub < P.n_sub; sub++) {
             for (int tile = lb; tile < D.tiles; tile += nb)
-                diffuse_tile<NSOL>(P, (tile % D.tiles_x) * kBX, (tile / D.tiles_x) * kBY, D.sph, D.sol[sidx],
+                diffuse_tile<NSOL, BY>(P, (tile % D.tiles_x) * kBX, (tile / D.tiles_x) * BY, D.sph, D.sol[sidx],
                                    D.sol[sidx ^ 1], sm.R);
             target += nb;
             if (!group_barrier(ctr + d, target, err, timeout_ns)) return;
@@ -200,23 +200,41 @@ __global__ void __launch_bounds__(kBT, 4) k_batch(const pf_batch_dom *__restrict
     }
 }
 
-}  // namespace
 
-int pf_batch_blocks_per_sm(int nsol) {
+template <int NSOL>
+int blocks_per_sm_ty(int by) {
     int nblk = 0;
-    cudaError_t e = nsol == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_batch<2>, kBT, 0)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_batch<1>, kBT, 0);
-    return e == cudaSuccess ? nblk : 0;
+    cudaError_t e = by == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_batch<NSOL, 4>, kBX * 4, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k_batch<NSOL, 8>, kBX * 8, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nblk;
 }
 
-int pf_batch_tile_cells() { return kBT; }
+template <int NSOL>
+cudaError_t launch_ty(int by, const cudaLaunchConfig_t &cfg, const pf_batch_dom *doms, const pf_f32_params *params,
+                      const int *block_dom, int nsteps, unsigned long long *ctr, int *err,
+                      unsigned long long timeout_ns) {
+    if (by == 4) return cudaLaunchKernelEx(&cfg, k_batch<NSOL, 4>, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
+    return cudaLaunchKernelEx(&cfg, k_batch<NSOL, 8>, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
+}
 
-cudaError_t pf_launch_batch(int nsol, int nblocks, const pf_batch_dom *doms, const pf_f32_params *params,
+}  // namespace
+
+int pf_batch_blocks_per_sm(int nsol, int tile_y) {
+    return nsol == 2 ? blocks_per_sm_ty<2>(tile_y) : blocks_per_sm_ty<1>(tile_y);
+}
+
+bool pf_batch_tile_ok(int tile_y) { return tile_y == 4 || tile_y == 8; }
+
+cudaError_t pf_launch_batch(int nsol, int tile_y, int nblocks, const pf_batch_dom *doms, const pf_f32_params *params,
                             const int *block_dom, int nsteps, unsigned long long *ctr, int *err,
                             unsigned long long timeout_ns, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)nblocks);
-    cfg.blockDim = dim3(kBT);
+    cfg.blockDim = dim3(kBX * tile_y);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -224,6 +242,6 @@ cudaError_t pf_launch_batch(int nsol, int nblocks, const pf_batch_dom *doms, con
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (nsol == 2) return cudaLaunchKernelEx(&cfg, k_batch<2>, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
-    return cudaLaunchKernelEx(&cfg, k_batch<1>, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
+    if (nsol == 2) return launch_ty<2>(tile_y, cfg, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
+    return launch_ty<1>(tile_y, cfg, doms, params, block_dom, nsteps, ctr, err, timeout_ns);
 }

@@ -57,55 +57,15 @@ __device__ __forceinline__ T pf_ld(const T *p) {
     return __ldg(p);
 }
 
-// Bulk test of Phase_field_solver (solver.cpp:207-216) for cell (i,j,k): one
-// grain above the cutoff here and the same single grain (and nothing else) in
-// every neighbour, so the merged stencil list holds one entry -- the cell is
-// copied to the output buffers (its phase planes stay as they are) and true is
-// returned.  Otherwise nothing is written.
-template <bool CG = false>
-__device__ __forceinline__ bool pf_phase_bulk(const pf_f32_params &P, int i, int j, int k,
-                                              const ushort4 *__restrict__ gid1, const float4 *__restrict__ phi1,
-                                              ushort4 *__restrict__ gid2, float4 *__restrict__ phi2) {
-    const int ix = P.ix, iy = P.iy, iz = P.iz;
-    const long long plane = (long long)ix * iy;
-    const long long n = i + (long long)ix * j + plane * k;
-    const ushort4 g = pf_ld<CG>(gid1 + n);
-    if (!(g.y == 0 && g.z == 0 && g.w == 0)) return false;
-    const float4 v = pf_ld<CG>(phi1 + n);
-    if (!(v.x > P.cutoff)) return false;
-    long long nb[6];
-    nb[0] = n - i + pf_wrap(i, ix, -1);
-    nb[1] = n - i + pf_wrap(i, ix, 1);
-    nb[2] = n + (long long)ix * (pf_wrap(j, iy, -1) - j);
-    nb[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
-    nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
-    nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
-    bool bulk = true;
-#pragma unroll
-    for (int b = 0; b < 6; b++)
-        if (b < P.nnb) {
-            const ushort4 ng = pf_ld<CG>(gid1 + nb[b]);
-            bulk = bulk && ng.x == g.x && ng.y == 0;
-        }
-    if (bulk) {
-        gid2[n] = g;
-        phi2[n] = v;
-    }
-    return bulk;
-}
-
 // Phase_field_solver (solver.cpp:147-304) for cell (i,j,k) on the compact FP32
-// layout; t is the thread's column in the shared list storage L.  The merged
-// stencil list is the cell's own slots above the cutoff (slot order) followed
-// by the grains its neighbours add, in the order met (solver.cpp:168-205).  Own
-// entries and their neighbour sums live in registers; only added grains are
-// searched in L.
+// layout; t is the thread's column in the shared list storage L.  Bulk cells
+// (a single grain in the stencil) are copied and keep their phase planes.
 template <int NSOL, int NT, bool CG = false>
-__device__ __forceinline__ void pf_phase_iface(const pf_f32_params &P, int i, int j, int k, int t,
-                                               const ushort4 *__restrict__ gid1, const float4 *__restrict__ phi1,
-                                               ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
-                                               float *__restrict__ sphase, const float2 *__restrict__ sol,
-                                               pf_plist<NT> &L) {
+__device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int j, int k, int t,
+                                              const ushort4 *__restrict__ gid1, const float4 *__restrict__ phi1,
+                                              ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
+                                              float *__restrict__ sphase, const float2 *__restrict__ sol,
+                                              pf_plist<NT> &L) {
     const int ix = P.ix, iy = P.iy, iz = P.iz;
     const long long plane = (long long)ix * iy;
     const long long n = i + (long long)ix * j + plane * k;
@@ -123,23 +83,41 @@ __device__ __forceinline__ void pf_phase_iface(const pf_f32_params &P, int i, in
     nb[3] = n + (long long)ix * (pf_wrap(j, iy, 1) - j);
     nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
     nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
-    // solver.cpp:168-177: own slots above the cutoff.
-    bool own[4];
-    float S[4];
-    int nown = 0;
+    // Fast path for the common bulk cell: one grain above the cutoff here and
+    // the same single grain (and nothing else) in every neighbour -- the merged
+    // stencil list would hold one entry (solver.cpp:207-216), so copy.
+    ushort4 ngid[6];
+#pragma unroll
+    for (int b = 0; b < 6; b++)
+        if (b < P.nnb) ngid[b] = pf_ld<CG>(gid1 + nb[b]);
+    if (g.y == 0 && g.z == 0 && g.w == 0 && v.x > cutoff) {
+        bool bulk = true;
+#pragma unroll
+        for (int b = 0; b < 6; b++)
+            if (b < P.nnb) bulk = bulk && ngid[b].x == g.x && ngid[b].y == 0;
+        if (bulk) {
+            gid2[n] = g;
+            phi2[n] = v;
+            return;
+        }
+    }
+    // solver.cpp:168-177: own slots above the cutoff (a sorted prefix).
+    int num = 0;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        own[a] = ov[a] > cutoff;
-        S[a] = 0.f;
-        nown += own[a] ? 1 : 0;
+        if (ov[a] > cutoff) {
+            L.id[num][t] = oid[a];
+            L.v1[num][t] = ov[a];
+            L.v2[num][t] = 0.f;
+            num++;
+        }
     }
-    int num = nown;
     // solver.cpp:179-205: merge the neighbours' lists (x-, x+, y-, y+, z-, z+),
-    // each scanned until its first empty slot; sums accumulate in visit order.
+    // each scanned until its first empty slot.
 #pragma unroll
     for (int b = 0; b < 6; b++) {
         if (b < P.nnb) {
-            const ushort4 ng = pf_ld<CG>(gid1 + nb[b]);
+            const ushort4 ng = ngid[b];
             const float4 nv4 = pf_ld<CG>(phi1 + nb[b]);
             const int nid[4] = {ng.x, ng.y, ng.z, ng.w};
             const float nv[4] = {nv4.x, nv4.y, nv4.z, nv4.w};
@@ -147,43 +125,23 @@ __device__ __forceinline__ void pf_phase_iface(const pf_f32_params &P, int i, in
             for (int a = 0; a < 4; a++) {
                 const int tid = nid[a];
                 if (tid == 0) break;
-                bool hit = false;
-#pragma unroll
-                for (int o = 0; o < 4; o++)
-                    if (own[o] && oid[o] == tid) {
-                        S[o] += nv[a];
-                        hit = true;
-                    }
-                if (!hit) {
-                    int kk = nown;
-                    while (kk < num && L.id[kk][t] != tid) kk++;
-                    if (kk < num) {
-                        L.v2[kk][t] += nv[a];
-                    } else if (num < PF_NSTENCIL) {
-                        L.id[num][t] = tid;
-                        L.v1[num][t] = 0.f;
-                        L.v2[num][t] = nv[a];
-                        num++;
-                    }
+                int kk = 0;
+                while (kk < num && L.id[kk][t] != tid) kk++;
+                if (kk < num) {
+                    L.v2[kk][t] += nv[a];
+                } else if (num < PF_NSTENCIL) {
+                    L.id[num][t] = tid;
+                    L.v1[num][t] = 0.f;
+                    L.v2[num][t] = nv[a];
+                    num++;
                 }
             }
         }
     }
-    if (num == 1) {  // solver.cpp:207-216: one entry, copy and leave the phase planes untouched
+    if (num == 1) {  // solver.cpp:207-216: bulk, copy and leave the phase planes untouched
         gid2[n] = g;
         phi2[n] = v;
         return;
-    }
-    {
-        int e = 0;
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-            if (own[a]) {
-                L.id[e][t] = oid[a];
-                L.v1[e][t] = ov[a];
-                L.v2[e][t] = S[a];
-                e++;
-            }
     }
     // Carbon concentration of each phase in this cell (for the driving force),
     // partitioned with the phase fractions of the current slots.
@@ -267,15 +225,4 @@ __device__ __forceinline__ void pf_phase_iface(const pf_f32_params &P, int i, in
     sphase[n] = sqrtf(ph[0] * inv);
     sphase[N + n] = sqrtf(ph[1] * inv);
     sphase[2 * N + n] = sqrtf(ph[2] * inv);
-}
-
-// The whole cell: bulk copy or the general update.
-template <int NSOL, int NT, bool CG = false>
-__device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int j, int k, int t,
-                                              const ushort4 *__restrict__ gid1, const float4 *__restrict__ phi1,
-                                              ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
-                                              float *__restrict__ sphase, const float2 *__restrict__ sol,
-                                              pf_plist<NT> &L) {
-    if (pf_phase_bulk<CG>(P, i, j, k, gid1, phi1, gid2, phi2)) return;
-    pf_phase_iface<NSOL, NT, CG>(P, i, j, k, t, gid1, phi1, gid2, phi2, sphase, sol, L);
 }

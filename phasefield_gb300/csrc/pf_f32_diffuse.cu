@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(32 * NTY, (32 * NTY) >= 512 ? 1 : 2)
 // the tile height, every tile's interior box lies inside the domain, so one
 // cp.async.bulk.tensor per array per plane brings it into shared memory: the
 // square-root phase planes as a (64, BY, 1, 3) box and the solute totals as a
-// (64 x BY) box.  A ring of kStages planes is kept in flight, each completing
+// (64 x BY) box.  A ring of 3 or 4 planes is kept in flight, each completing
 // on its own mbarrier, so HBM latency is covered by copies in flight rather
 // than by registers or resident warps.  The halo ring is loaded with plain
 // loads one plane ahead, as in variant 0.  Arithmetic, and so every result bit,
@@ -453,7 +453,6 @@ __global__ void __launch_bounds__(32 * NTY, (32 * NTY) >= 512 ? 1 : 2)
 // (no thread leaves early, so no barrier is left waiting), and before exiting
 // waits once more, again bounded, for its own copies still in flight.
 // ---------------------------------------------------------------------------
-constexpr int kStages = 4;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -474,7 +473,7 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
 // Bounded wait for one phase of a stage barrier; false when it ran out.
@@ -504,25 +503,29 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, i
 
 __device__ int g_diffuse_timeout;
 
-template <int NSOL, int NPF, int RY, int NTY>
+// NST planes in the ring; NRB record buffers (2: one barrier per plane, 1: a
+// second barrier per plane but half the record storage, which lets two
+// 16-row blocks share an SM).
+template <int NSOL, int NPF, int RY, int NTY, int NST, int NRB>
 struct TmaShape {
     using B = Shape<NSOL, NPF, 6, RY, NTY>;
     static constexpr int BY = B::BY;
     static constexpr size_t s_bytes = 3ull * BY * kBX * sizeof(float);                 // phase planes of one plane
     static constexpr size_t v_bytes = (size_t)BY * kBX * sizeof(typename SolVec<NSOL>::T);  // solute totals
     static constexpr size_t stage = ((s_bytes + v_bytes + 127) / 128) * 128;
-    static constexpr size_t rec_off = kStages * stage;
-    static constexpr size_t bar_off = rec_off + ((B::bytes + 127) / 128) * 128;
-    static constexpr size_t bytes = bar_off + kStages * sizeof(unsigned long long) + 128;  // + alignment slack
+    static constexpr size_t rec_off = NST * stage;
+    static constexpr size_t bar_off = rec_off + ((B::bytes * NRB / 2 + 127) / 128) * 128;
+    static constexpr size_t bytes = bar_off + NST * sizeof(unsigned long long) + 128;  // + alignment slack
 };
 
-template <int NSOL, int NPF, int RY, int NTY>
+template <int NSOL, int NPF, int RY, int NTY, int NST, int NRB>
 __global__ void __launch_bounds__(32 * NTY, 2)
     k_diffuse_tma(const __grid_constant__ pf_f32_params P, const __grid_constant__ CUtensorMap tm_s,
                   const __grid_constant__ CUtensorMap tm_v, const float *__restrict__ sphase,
                   const float2 *__restrict__ sol_in, float2 *__restrict__ sol_out, int zchunk) {
-    using T = TmaShape<NSOL, NPF, RY, NTY>;
+    using T = TmaShape<NSOL, NPF, RY, NTY, NST, NRB>;
     using S = typename T::B;
+    constexpr int kStages = NST;
     using SV = typename SolVec<NSOL>::T;
     using RB = typename RecB<NSOL, NPF>::T;
     constexpr int BY = S::BY, ROWS = S::ROWS;
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(32 * NTY, 2)
     unsigned char *smem_raw =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
     float4 *recA = reinterpret_cast<float4 *>(smem_raw + T::rec_off);
-    RB *recB = reinterpret_cast<RB *>(smem_raw + T::rec_off + S::bytes_a);
+    RB *recB = reinterpret_cast<RB *>(smem_raw + T::rec_off + S::bytes_a * NRB / 2);
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem_raw + T::bar_off);
     auto slot = [](int buf, int row, int par, int col) { return ((buf * ROWS + row) * 2 + par) * kCols + col; };
     auto stage_s = [&](int st) { return reinterpret_cast<const float *>(smem_raw + st * T::stage); };
@@ -646,7 +649,7 @@ __global__ void __launch_bounds__(32 * NTY, 2)
 
     for (int z = z0; z < z1; z++) {
         const int pl = z - z0 + 1;
-        const int buf = (z - z0) & 1;
+        const int buf = NRB == 2 ? (z - z0) & 1 : 0;
 #pragma unroll
         for (int ry = 0; ry < RY; ry++)
 #pragma unroll
@@ -749,6 +752,7 @@ __global__ void __launch_bounds__(32 * NTY, 2)
                 else solo[off + col[ry][rx]] = make_float2(o[0], o[1]);
                 cur[ry][rx] = nxt[ry][rx];
             }
+        if (NRB == 1) __syncthreads();  // the single record buffer is rewritten next plane
     }
     if (!ok) {
         atomicExch(&g_diffuse_timeout, 1);
@@ -840,14 +844,18 @@ bool tma_ok(const pf_f32_params &P, int by) {
 template <int NSOL, int NPF, int BY>
 cudaError_t launch_tma(const pf_f32_params &P, const float *sphase, const float2 *sol_in, float2 *sol_out,
                        cudaStream_t s, int zchunk) {
-    constexpr int RY = BY == 8 ? 1 : 2, NTY = 8;
-    using T = TmaShape<NSOL, NPF, RY, NTY>;
+    // A 4-plane ring with double-buffered records: about 85 KB of shared
+    // memory for 8-row tiles (two blocks per SM), 164 KB for 16-row tiles (one
+    // block per SM; measured faster on GB300 than a 3-plane ring with a single
+    // record buffer, which fits two).
+    constexpr int RY = BY == 8 ? 1 : 2, NTY = 8, NST = 4, NRB = 2;
+    using T = TmaShape<NSOL, NPF, RY, NTY, NST, NRB>;
     CUtensorMap ms, mv;
     if (!tensor_map(sphase, P.ix, P.iy, P.iz, BY, 0, &ms) || !tensor_map(sol_in, P.ix, P.iy, P.iz, BY, NSOL, &mv))
         return cudaErrorInvalidValue;
     const int tiles = (P.ix / kBX) * (P.iy / BY);
     const dim3 grid((unsigned)tiles, (unsigned)((P.iz + zchunk - 1) / zchunk));
-    auto kern = k_diffuse_tma<NSOL, NPF, RY, NTY>;
+    auto kern = k_diffuse_tma<NSOL, NPF, RY, NTY, NST, NRB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::bytes);
     if (e != cudaSuccess) return e;
     kern<<<grid, 32 * NTY, T::bytes, s>>>(P, ms, mv, sphase, sol_in, sol_out, zchunk);

@@ -57,12 +57,13 @@ struct pf_batch_dom {
     float2 *sol[2];
     int cur, curs;          // buffer roles at the start of the launch
     int nb_first, nb;       // the domain's block group
-    int tiles_x, tiles;     // 32x8 tiles of the domain
+    int tiles_x, tiles;     // 32 x tile_y tiles of the domain
     int extra_target;       // test knob: > 0 makes the group barriers unreachable
 };
-int pf_batch_blocks_per_sm(int nsol);
-int pf_batch_tile_cells();
-cudaError_t pf_launch_batch(int nsol, int nblocks, const pf_batch_dom *doms, const pf_f32_params *params,
+// Tiles are 32 x tile_y cells, tile_y 4 or 8 (pf_batch_tile_ok).
+int pf_batch_blocks_per_sm(int nsol, int tile_y);
+bool pf_batch_tile_ok(int tile_y);
+cudaError_t pf_launch_batch(int nsol, int tile_y, int nblocks, const pf_batch_dom *doms, const pf_f32_params *params,
                             const int *block_dom, int nsteps, unsigned long long *ctr, int *err,
                             unsigned long long timeout_ns, cudaStream_t s);
 

@@ -73,3 +73,67 @@ def test_batch_rejects_3d_and_mixed_solutes(gpu, tmp_path):
     m1 = pf.read_model(W.write_config(str(tmp_path / "c1.txt"), grid=(32, 32, 1), mn=False))
     with pytest.raises(pf.PfError):
         pf.Batch([models[0], m1])
+
+
+def test_batch_matches_oracle(gpu, tmp_path):
+    """Two domains of one persistent launch against the FP64 CPU oracle (the
+    six-slot reference algorithm) on the same inputs: the tolerances of the
+    single-domain FP32C-vs-FP64 test (near-equilibrium carbon): mean |dphase|
+    <= 2e-4, phase fractions within 1e-4, total carbon within 1e-4 relative
+    max-norm."""
+    import os
+
+    import pyoracle as po
+    from helpers import copy_state, rel_maxnorm
+
+    models, states = _domains(tmp_path)
+    B = pf.Batch(models)
+    for d, st in enumerate(states):
+        B.upload(d, st, 0.0)
+    steps = 12
+    assert B.run(steps) == pf.PF_OK
+    paths = sorted(p for p in os.listdir(tmp_path) if p.startswith("ens") and p.endswith(".txt"))
+    for d in (0, 2):
+        m = models[d]
+        N = m.ix * m.iy
+        om = po.load_model(os.path.join(str(tmp_path), paths[d]))
+        ref = copy_state(states[d])
+        t = po.run(om, ref, 0.0, steps)
+        got = B.download(d)
+        assert got["time"] == t
+        dphase = np.abs(got["phase"] - ref["phase"])
+        fr_b = got["phase"].reshape(N, 3).mean(0)
+        fr_o = ref["phase"].reshape(N, 3).mean(0)
+        print(f"domain {d}: mean|dphase| {dphase.mean():.2e}, fractions {fr_b[:2]} vs {fr_o[:2]}")
+        assert dphase.mean() <= 2e-4
+        np.testing.assert_allclose(fr_b, fr_o, atol=1e-4)
+        assert rel_maxnorm(got["C"][:N], ref["C"][:N]) <= 1e-4
+
+
+def test_batch_tile_shapes_agree_and_autotune_restores(gpu, tmp_path):
+    """Every tile shape gives bit-identical states; the autotuner leaves the
+    ensemble exactly where it found it."""
+    models, states = _domains(tmp_path, gentle=False)
+    out = {}
+    for ty, div in ((8, 1), (4, 1), (4, 2)):
+        B = pf.Batch(models)
+        for d, st in enumerate(states):
+            B.upload(d, st, 0.0)
+        B.set_tile(ty, div)
+        assert B.run(6) == pf.PF_OK
+        out[(ty, div)] = [B.download(d) for d in range(len(models))]
+        B.close()
+    for key, res in out.items():
+        for d in range(len(models)):
+            for k in ("ids", "phi", "phase", "C"):
+                assert np.array_equal(res[d][k], out[(8, 1)][d][k]), (key, d, k)
+    B = pf.Batch(models)
+    for d, st in enumerate(states):
+        B.upload(d, st, 0.0)
+    best = B.autotune(3)
+    assert best["tile_y"] in (4, 8) and best["ms"] > 0
+    assert B.run(6) == pf.PF_OK
+    for d in range(len(models)):
+        got = B.download(d)
+        for k in ("ids", "phi", "phase", "C"):
+            assert np.array_equal(got[k], out[(8, 1)][d][k]), (d, k)
