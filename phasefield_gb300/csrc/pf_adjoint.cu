@@ -28,8 +28,11 @@
 //   cell; the neighbour sums S_e = sum_nb phi_nb(e) are returned to the
 //   neighbours' slots by a gather over the neighbours' published lists.
 // Checkpoints every K steps; a segment is recomputed forward storing every
-// step's pre-step state and every sub-step's derived planes (s_p, c_p, 1/t1_p;
-// HBM is plentiful), then swept backwards.  Full segments are replayed from one
+// step's pre-step state and the carbon after each diffusion sub-step, then
+// swept backwards; the derived quantities (s_p, c_p, 1/t1_p) are recomputed
+// from those where needed, which costs far less than storing and reloading
+// them.  The reverse diffusion sub-steps of a step run as one cooperative
+// launch with bounded grid barriers.  Full segments are replayed from one
 // captured CUDA graph.
 #include <cmath>
 #include <cstring>
@@ -42,6 +45,8 @@
 namespace {
 
 constexpr int LMAX = PF_NSTENCIL;
+constexpr int kCoopCells = 4;                              // cells per thread of the cooperative reverse diffusion
+constexpr unsigned long long kCoopTimeoutNs = 2000000000ull;  // its barrier wait limit
 
 template <typename R>
 struct AP {
@@ -56,6 +61,24 @@ struct AP {
 
 __device__ __forceinline__ int lphase(int l, int b1, int b2) { return l == 0 ? 0 : (l <= b1 ? 1 : (l <= b2 ? 2 : 3)); }
 
+
+// Sum of v over the block (blockDim.x == PF_CELL_THREADS), added to *dst by
+// one atomic per block instead of one per warp (the gradient accumulators are
+// a handful of doubles that every block of a launch hits).  Every thread of
+// the block must call it.
+__device__ __forceinline__ void block_add(double v, double *dst) {
+    __shared__ double part[PF_CELL_THREADS / 32];
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+    const int w = threadIdx.x >> 5;
+    __syncthreads();  // part[] may still be read by a previous call
+    if ((threadIdx.x & 31) == 0) part[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < PF_CELL_THREADS / 32; k++) t += part[k];
+        if (t != 0) atomicAdd(dst, t);
+    }
+}
 
 template <typename R>
 __device__ __forceinline__ void partition(const AP<R> &P, R C, const R ph[3], R c[3], R t1[3]) {
@@ -160,24 +183,35 @@ __device__ void build_list(const AP<R> &P, int ci, int cj, int ck, long long n, 
 }
 
 // ---------------------------------------------------------------- forward --
-// Derived planes of one cell for one sub-step: s_p = sqrt(phi_p), c_p
-// (partitioned carbon) and 1/t1_p, each stored as three planes.
+// Derived quantities of a step's diffusion.  With the phase fractions fixed
+// over the step, s_p = sqrt(phi_p), 1/t1_p and t2_p (t1_p = sum_j phi_j k_pj,
+// t2_p = sum_j phi_j c_pj) are computed once per step and kept as planes
+// (DS: 9N values, planes s, 1/t1, t2 for p = 0..2); each sub-step then gets
+// the partitioned carbon c_p = (C - t2_p) / t1_p as (C - t2_p) * (1/t1_p), a
+// single multiply-add, forward and reverse alike.
 template <typename R>
-__device__ __forceinline__ void derive_cell(const AP<R> &P, long long n, const R p[3], R C, R *ds, R *dc, R *dit) {
-    R c[3], t[3];
-    partition(P, C, p, c, t);
-    for (int q = 0; q < 3; q++) {
-        ds[q * P.N + n] = sqrt(p[q]);
-        dc[q * P.N + n] = c[q];
-        dit[q * P.N + n] = (R)1 / t[q];
+__device__ __forceinline__ void step_planes(const AP<R> &P, long long n, const R p[3], R *DS) {
+    for (int i = 0; i < 3; i++) {
+        R a = 0, b = 0;
+        for (int j = 0; j < 3; j++) {
+            a += p[j] * P.k[i + 3 * j];
+            b += p[j] * P.c[i + 3 * j];
+        }
+        DS[i * P.N + n] = sqrt(p[i]);
+        DS[(3 + i) * P.N + n] = (R)1 / a;
+        DS[(6 + i) * P.N + n] = b;
     }
 }
+template <typename R>
+__device__ __forceinline__ R cpart(const AP<R> &P, const R *DS, int p, long long n, R C) {
+    return (C - DS[(6 + p) * P.N + n]) * DS[(3 + p) * P.N + n];
+}
 
-// Phase sweep; also writes the derived planes of the first diffusion sub-step
-// (the new phase fractions with the unchanged carbon).
+// Phase sweep; also writes the step's diffusion planes (step_planes) of the
+// new phase fractions.
 template <typename R>
 __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
-                            R *phi2, R *ph2, R *ds, R *dc, R *dit) {
+                            R *phi2, R *ph2, R *DS) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
@@ -188,7 +222,7 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
         for (int a = 0; a < 4; a++) phi2[4 * n + a] = phi[4 * n + a];
         const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
         for (int p = 0; p < 3; p++) ph2[3 * n + p] = pp[p];
-        derive_cell(P, n, pp, C[n], ds, dc, dit);
+        step_planes(P, n, pp, DS);
         return;
     }
     const R inv = (R)1 / L.sum;
@@ -210,81 +244,205 @@ __global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, con
         pp[p] = q[p] * inv;
         ph2[3 * n + p] = pp[p];
     }
-    derive_cell(P, n, pp, C[n], ds, dc, dit);
+    step_planes(P, n, pp, DS);
 }
 
-// Forward sub-step (solver.cpp:343-372) from the derived planes:
-//   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p);
-// with ds2 != NULL it also writes the next sub-step's derived planes.
+// Forward sub-step (solver.cpp:343-372):
+//   C' = C + sum_p s_p D_p sum_nb s_p^nb (c_p^nb - c_p),
+// from the step's planes DS and C.  Cst, when given, receives a copy of C'
+// (the reverse sweep's record of this sub-step).  Phases with D_p = 0
+// contribute exactly zero and are skipped.
 template <typename R>
-__global__ void k_fwd_diffuse_d(const AP<R> P, const R *ds, const R *dc, const R *C, R *C2, const R *ph, R *ds2,
-                                R *dc2, R *dit2) {
+__global__ void k_fwd_diffuse_d(const AP<R> P, const R *DS, const R *C, R *C2, R *Cst) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nb[6];
     pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
+    const R C0 = C[n];
     R f = 0;
     for (int p = 0; p < 3; p++) {
-        const R c0 = dc[p * P.N + n];
+        if (P.D[p] == (R)0) continue;
+        const R c0 = cpart(P, DS, p, n, C0);
         R a = 0;
         // The diffusion sums carry no discrete decision: fused multiply-adds
         // are used explicitly (this file is otherwise built without contraction).
-        for (int b = 0; b < P.nnb; b++) a = fma(ds[p * P.N + nb[b]], dc[p * P.N + nb[b]] - c0, a);
-        f = fma(ds[p * P.N + n] * P.D[p], a, f);
+        for (int b = 0; b < P.nnb; b++) {
+            const long long m = nb[b];
+            a = fma(DS[p * P.N + m], cpart(P, DS, p, m, C[m]) - c0, a);
+        }
+        f = fma(DS[p * P.N + n] * P.D[p], a, f);
     }
-    const R cn = C[n] + f;
+    const R cn = C0 + f;
     C2[n] = cn;
-    if (ds2) {
-        const R pp[3] = {ph[3 * n], ph[3 * n + 1], ph[3 * n + 2]};
-        derive_cell(P, n, pp, cn, ds2, dc2, dit2);
-    }
+    if (Cst) Cst[n] = cn;
 }
 
-// Reverse of one diffusion sub-step.  In: lam (adjoint of C after the
-// sub-step), the derived planes of the state before it, ph.  Out: lam2
-// (adjoint of C before), lph += the phase-fraction part (through s_p and
-// c_p(phi)), grad[2] += dJ/ds_C.
+// Reverse of one diffusion sub-step for cell n.  In: lam (adjoint of C after
+// the sub-step; read through L2 when LCG, i.e. when other blocks of the same
+// launch wrote it), the step's planes DS and the carbon Cin before the
+// sub-step.  Returns the adjoint of C before the sub-step; adds the
+// phase-fraction part (through s_p and c_p(phi)) to lph_add and s_C * dJ/ds_C
+// to g (kept in the working precision per thread: FP64 arithmetic is scarce
+// on GB300; the block sums are FP64).
+template <typename R, bool LCG>
+__device__ __forceinline__ R bwd_diffuse_cell(const AP<R> &P, long long n, const long long nb[6], const R *DS,
+                                              const R *Cin, const R *lam, R lph_add[3], R &g) {
+    auto ld = [&](const R *p) { return LCG ? __ldcg(p) : *p; };
+    const R l0 = ld(lam + n);
+    const R C0 = Cin[n];
+    R out = l0, dL_ds[3], dL_dc[3], c0s[3], it0[3], s0s[3], flux = 0;
+    for (int p = 0; p < 3; p++) {
+        dL_ds[p] = dL_dc[p] = c0s[p] = it0[p] = s0s[p] = 0;
+        if (P.D[p] == (R)0) continue;  // no flux, no derivative
+        const R s0 = DS[p * P.N + n], c0 = cpart(P, DS, p, n, C0);
+        R al = 0, ac = 0, ads = 0;
+        for (int b = 0; b < P.nnb; b++) {
+            const long long m = nb[b];
+            const R sm = DS[p * P.N + m], dcm = cpart(P, DS, p, m, Cin[m]) - c0, lm = ld(lam + m);
+            al = fma(sm, lm - l0, al);
+            ac = fma(sm, dcm, ac);
+            ads = fma(sm * dcm, l0 - lm, ads);
+        }
+        it0[p] = DS[(3 + p) * P.N + n];
+        c0s[p] = c0;
+        s0s[p] = s0;
+        out = fma(P.D[p] * s0 * it0[p], al, out);
+        dL_dc[p] = P.D[p] * s0 * al;
+        dL_ds[p] = P.D[p] * ads;
+        flux = fma(s0 * P.D[p], ac, flux);
+    }
+    for (int j = 0; j < 3; j++) {
+        R v = 0;
+        for (int p = 0; p < 3; p++)
+            if (P.D[p] != (R)0) v += dL_dc[p] * (-(P.c[p + 3 * j] + c0s[p] * P.k[p + 3 * j]) * it0[p]);
+        if (s0s[j] > (R)0) v += dL_ds[j] / ((R)2 * s0s[j]);
+        lph_add[j] += v;
+    }
+    g = fma(l0, flux, g);
+    return out;
+}
+
+// Reverse of one diffusion sub-step (one launch per sub-step).  Out: lam2,
+// lph += the phase-fraction part, grad[2] += dJ/ds_C.
 template <typename R>
-__global__ void k_bwd_diffuse_d(const AP<R> P, const R *ph, const R *ds, const R *dc, const R *dit, const R *lam,
-                                R *lam2, R *lph, double *grad) {
+__global__ void k_bwd_diffuse_d(const AP<R> P, const R *DS, const R *Cin, const R *lam, R *lam2, R *lph,
+                                double *grad) {
     int ci, cj, ck;
     long long n;
     const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
-    double g = 0;
+    R g = 0;
     if (in) {
         long long nb[6];
         pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
-        const R l0 = lam[n];
-        R out = l0, dL_ds[3], dL_dc[3], flux = 0;
-        for (int p = 0; p < 3; p++) {
-            const R s0 = ds[p * P.N + n], c0 = dc[p * P.N + n];
-            R al = 0, ac = 0, ads = 0;
-            for (int b = 0; b < P.nnb; b++) {
-                const long long m = nb[b];
-                const R sm = ds[p * P.N + m], dcm = dc[p * P.N + m] - c0, lm = lam[m];
-                al = fma(sm, lm - l0, al);
-                ac = fma(sm, dcm, ac);
-                ads = fma(sm * dcm, l0 - lm, ads);
-            }
-            out = fma(P.D[p] * s0 * dit[p * P.N + n], al, out);
-            dL_dc[p] = P.D[p] * s0 * al;
-            dL_ds[p] = P.D[p] * ads;
-            flux = fma(s0 * P.D[p], ac, flux);
-        }
-        lam2[n] = out;
-        for (int j = 0; j < 3; j++) {
-            R v = 0;
-            for (int p = 0; p < 3; p++)
-                v += dL_dc[p] * (-(P.c[p + 3 * j] + dc[p * P.N + n] * P.k[p + 3 * j]) * dit[p * P.N + n]);
-            const R sj = ds[j * P.N + n];
-            if (sj > (R)0) v += dL_ds[j] / ((R)2 * sj);
-            lph[3 * n + j] += v;
-        }
-        g = (double)l0 * (double)flux / (double)P.s_c;
+        R add[3] = {0, 0, 0};
+        lam2[n] = bwd_diffuse_cell<R, false>(P, n, nb, DS, Cin, lam, add, g);
+        for (int j = 0; j < 3; j++) lph[3 * n + j] += add[j];
     }
-    for (int s = 16; s > 0; s >>= 1) g += __shfl_down_sync(0xffffffffu, g, s);
-    if ((threadIdx.x & 31) == 0 && g != 0) atomicAdd(grad + 2, g);
+    block_add((double)g / (double)P.s_c, grad + 2);
+}
+
+__device__ __forceinline__ unsigned long long adj_globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier among all blocks of a cooperative launch (all resident).  The wait
+// is bounded by a wall-clock limit: a block that waits longer sets *err, and
+// every block leaves at its next barrier.  Returns false when leaving.
+__device__ __forceinline__ bool adj_grid_barrier(unsigned long long *ctr, unsigned long long target, int *err,
+                                                 unsigned long long timeout_ns) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1ull);
+        const unsigned long long t0 = adj_globaltimer();
+        int good = 1;
+        while (true) {
+            if (atomicAdd(ctr, 0ull) >= target) break;
+            if (*(volatile int *)err) { good = 0; break; }
+            if (adj_globaltimer() - t0 > timeout_ns) {
+                atomicExch(err, 1);
+                good = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// gather_cell (the neighbour part of the reverse phase sweep) is defined below.
+template <typename R>
+__device__ __forceinline__ void gather_cell(const AP<R> &P, long long m, const long long nb[6], const ushort4 *gid,
+                                            const int *pub_id, const R *pub_l, R *lphi_pre);
+
+// All n_sub reverse diffusion sub-steps of one step in one cooperative
+// launch: each thread keeps up to CPT cells (grid-stride), their phase-fraction
+// adjoints accumulate in registers across the sub-steps, and the sub-steps are
+// separated by a grid barrier.  lam starts in lamA; the result lands in lamA
+// for an even n_sub, lamB for an odd one (as with one launch per sub-step).
+// The carbon before sub-step k is C0 (k = 0) or Csub + N (k - 1).
+// With gat_gid != NULL the launch first completes the neighbour part of the
+// previous reverse step's phase sweep (gather_cell into gat_lphi): it touches
+// other data than the diffusion, so it needs no barrier.
+template <typename R, int CPT>
+__global__ void __launch_bounds__(PF_CELL_THREADS) k_bwd_diffuse_all(const AP<R> P, const R *DS, const R *C0,
+                                                                     const R *Csub, R *lamA, R *lamB, R *lph,
+                                                                     double *grad, unsigned long long *ctr, int *err,
+                                                                     unsigned long long timeout_ns,
+                                                                     const ushort4 *gat_gid, const int *pub_id,
+                                                                     const R *pub_l, R *gat_lphi) {
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gat_gid)
+        for (int c = 0; c < CPT; c++) {
+            const long long n = t + c * T;
+            if (n < P.N) {
+                const int plane = P.ix * P.iy;
+                const int ck = (int)(n / plane), rem = (int)(n - (long long)ck * plane);
+                const int cj = rem / P.ix, ci = rem - cj * P.ix;
+                long long nb[6];
+                pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
+                gather_cell(P, n, nb, gat_gid, pub_id, pub_l, gat_lphi);
+            }
+        }
+    R add[CPT][3];
+    for (int c = 0; c < CPT; c++) add[c][0] = add[c][1] = add[c][2] = 0;
+    R g = 0;
+    R *lin = lamA, *lout = lamB;
+    unsigned long long target = 0;
+    bool alive = true;
+    for (int k = P.n_sub - 1; k >= 0 && alive; k--) {
+        const R *Cin = k == 0 ? C0 : Csub + (size_t)P.N * (k - 1);
+        for (int c = 0; c < CPT; c++) {
+            const long long n = t + c * T;
+            if (n < P.N) {
+                const int plane = P.ix * P.iy;
+                const int ck = (int)(n / plane), rem = (int)(n - (long long)ck * plane);
+                const int cj = rem / P.ix, ci = rem - cj * P.ix;
+                long long nb[6];
+                pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nb);
+                lout[n] = bwd_diffuse_cell<R, true>(P, n, nb, DS, Cin, lin, add[c], g);
+            }
+        }
+        R *tmp = lin; lin = lout; lout = tmp;
+        if (k > 0) {
+            target += gridDim.x;
+            alive = adj_grid_barrier(ctr, target, err, timeout_ns);
+        }
+    }
+    for (int c = 0; c < CPT; c++) {
+        const long long n = t + c * T;
+        if (n < P.N)
+            for (int j = 0; j < 3; j++) lph[3 * n + j] += add[c][j];
+    }
+    block_add((double)g / (double)P.s_c, grad + 2);
 }
 
 // Objective sums in FP64: out[0] = sum phi_1, out[1] = sum phi_2, out[2] = sum phi_2 c_2.
@@ -350,7 +508,7 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
     int ci, cj, ck;
     long long n;
     const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
-    double gm = 0, gs = 0;
+    R gm = 0, gs = 0;  // s_m dJ/ds_m and s_sigma dJ/ds_sigma of this cell
     if (in) {
         Lst<R> L;
         build_list(P, ci, cj, ck, n, gid, phi, C, L);
@@ -408,8 +566,8 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
                     lv1[f] += le * (P.A[x] * L.S[e] - P.B[x] + P.G[x] * Q * dZf);
                     lc[pe - 1] += le * P.G[x] * Z;
                     const R T = P.A[x] * X + P.B[x] * Y + P.G[x] * Z * Q;
-                    gm += (double)le * (double)T / (double)P.s_m;
-                    gs += (double)le * (double)(P.A[x] * X + P.B[x] * Y) / (double)P.s_s;
+                    gm = fma(le, T, gm);
+                    gs = fma(le, P.A[x] * X + P.B[x] * Y, gs);
                 }
             }
             // Carbon partition of the driving force: c_p(C, ph_old).
@@ -436,26 +594,16 @@ __global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi,
             if (L.num < LMAX) pub_id[LMAX * n + L.num] = 0;  // terminator (the gather stops at id 0)
         }
     }
-    for (int s = 16; s > 0; s >>= 1) {
-        gm += __shfl_down_sync(0xffffffffu, gm, s);
-        gs += __shfl_down_sync(0xffffffffu, gs, s);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (gm != 0) atomicAdd(grad + 0, gm);
-        if (gs != 0) atomicAdd(grad + 1, gs);
-    }
+    block_add((double)gm / (double)P.s_m, grad + 0);
+    block_add((double)gs / (double)P.s_s, grad + 1);
 }
 
 // Reverse of the phase sweep, neighbour part: every slot of cell m that its
 // neighbours scanned (up to the first empty slot) receives the neighbours'
 // published adjoint of their stencil sum for that grain.
 template <typename R>
-__global__ void k_bwd_phase_gather(const AP<R> P, const ushort4 *gid, const int *pub_id, const R *pub_l, R *lphi_pre) {
-    int ci, cj, ck;
-    long long m;
-    if (!pf_cell(P.ix, P.iy, ci, cj, ck, m)) return;
-    long long nb[6];
-    pf_neighbours3(ci, cj, ck, m, P.ix, P.iy, P.iz, nb);
+__device__ __forceinline__ void gather_cell(const AP<R> &P, long long m, const long long nb[6], const ushort4 *gid,
+                                            const int *pub_id, const R *pub_l, R *lphi_pre) {
     const ushort4 g = gid[m];
     const int id[4] = {g.x, g.y, g.z, g.w};
     R add[4] = {0, 0, 0, 0};
@@ -471,6 +619,16 @@ __global__ void k_bwd_phase_gather(const AP<R> P, const ushort4 *gid, const int 
         }
     }
     for (int a = 0; a < 4; a++) lphi_pre[4 * m + a] += add[a];
+}
+
+template <typename R>
+__global__ void k_bwd_phase_gather(const AP<R> P, const ushort4 *gid, const int *pub_id, const R *pub_l, R *lphi_pre) {
+    int ci, cj, ck;
+    long long m;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, m)) return;
+    long long nb[6];
+    pf_neighbours3(ci, cj, ck, m, P.ix, P.iy, P.iz, nb);
+    gather_cell(P, m, nb, gid, pub_id, pub_l, lphi_pre);
 }
 
 // Reference layout -> calibration layout (carbon only; at most 4 slots kept).
@@ -521,16 +679,21 @@ struct AdjCtx : pf_adj_impl {
     std::vector<R *> ck_phi, ck_ph, ck_C;
     // segment storage: per step pre-step state and pre-sub-step carbon
     std::vector<ushort4 *> sg_gid;
-    std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;
+    std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;  // sg_Csub: each step's diffusion record
+    R *dscr = nullptr;  // the step planes of a forward run without records (9N)
     ushort4 *w_gid = nullptr, *v_gid = nullptr;  // w_*, v_*: the forward's two state sets
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
     R *v_phi = nullptr, *v_ph = nullptr, *v_C = nullptr;
-    R *dscr = nullptr;  // two scratch slots of derived planes (9N each)
     // adjoint buffers
     R *l_phi = nullptr, *l_ph = nullptr, *l_C = nullptr, *l_phi2 = nullptr, *l_ph2 = nullptr, *l_C2 = nullptr;
     int *pub_id = nullptr;
     R *pub_l = nullptr;
     double *d_acc = nullptr;  // 3 objective sums + 4 gradient components
+    // Cooperative reverse diffusion (all sub-steps of a step in one launch):
+    // barrier counter, error flag, resident-block capacity.
+    unsigned long long *d_ctr = nullptr;
+    int *d_err = nullptr;
+    int coop_blocks = 0;
     double J[2] = {0, 0}, W = 0;
     double ms_fwd = 0, ms_bwd = 0;
     pf_f32_map map{};
@@ -559,6 +722,7 @@ struct AdjCtx : pf_adj_impl {
         f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(dscr);
         f(v_gid); f(v_phi); f(v_ph); f(v_C);
         f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
+        f(d_ctr); f(d_err);
         if (s) cudaStreamDestroy(s);
     }
 
@@ -590,26 +754,29 @@ struct AdjCtx : pf_adj_impl {
         n_sub = p.n_sub;
     }
 
-    // One forward step.  With Dsub (n_sub * 9N values) the derived planes of
-    // every sub-step (s_p, c_p, 1/t1_p) are kept there for the reverse sweep.
+    // The reverse sweep's record of one step's diffusion: the step's planes
+    // (9N, step_planes) and the carbon after sub-steps 0 .. n_sub-2 (the
+    // carbon before sub-step 0 is the stored pre-step state, the last
+    // sub-step's result is the next step's).
+    static size_t record_size(int nsub, size_t n) { return (size_t)(9 + (nsub > 1 ? nsub - 1 : 0)) * n; }
+
+    // One forward step; with Drec (record_size values) the step's diffusion
+    // record is kept there for the reverse sweep, else the planes go to the
+    // scratch.
     int step(const ushort4 *g, const R *phi, const R *ph, const R *C, ushort4 *g2, R *phi2, R *ph2, R *C2,
-             R *Dsub) {
+             R *Drec) {
         const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
-        // Derived planes of sub-step k: slot k of Dsub, or one of two scratch
-        // slots used alternately.
-        auto slot = [&](int k) -> R * { return Dsub ? Dsub + (size_t)k * 9 * N : dscr + (size_t)(k & 1) * 9 * N; };
-        R *d0 = slot(0);
-        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, d0, d0 + 3 * N, d0 + 6 * N);
+        R *DS = Drec ? Drec : dscr;
+        R *Csub = Drec ? Drec + 9 * N : nullptr;
+        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, DS);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
         // one lands in C2 and no sub-step reads the buffer it writes.
         R *buf[2] = {C2, w_C2};
         const R *cin = C;
         for (int k = 0; k < n_sub; k++) {
             R *cout = buf[(n_sub - 1 - k) % 2];
-            R *dk = slot(k);
-            R *dn = (k + 1 < n_sub) ? slot(k + 1) : nullptr;
-            k_fwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, dk, dk + 3 * N, cin, cout, ph2, dn, dn ? dn + 3 * N : nullptr,
-                                                  dn ? dn + 6 * N : nullptr);
+            k_fwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, DS, cin, cout,
+                                                              Csub && k + 1 < n_sub ? Csub + (size_t)k * N : nullptr);
             cin = cout;
         }
         return cudaGetLastError() == cudaSuccess ? PF_OK : pf_fail(PF_ERR_CUDA, "adjoint forward launch");
@@ -624,6 +791,42 @@ struct pf_adj {
 template <typename R>
 static AdjCtx<R> *as(pf_adj *a) { return static_cast<AdjCtx<R> *>(a->impl); }
 
+// The reverse diffusion sub-steps of one step: one cooperative launch when
+// every cell fits kCoopCells per resident thread, else one launch per
+// sub-step.  The adjoint of C ends in the same buffer either way.
+template <typename R>
+static void bwd_diffusion(AdjCtx<R> *c, const AP<R> &P, const R *Drec, const R *C0, const ushort4 *gat_gid,
+                          R *gat_lphi) {
+    const size_t N = (size_t)c->N;
+    const R *DS = Drec, *Csub = Drec + 9 * N;
+    const long long need = (c->N + PF_CELL_THREADS - 1) / PF_CELL_THREADS;
+    const long long blocks = need < c->coop_blocks ? need : c->coop_blocks;
+    if (blocks > 0 && blocks * PF_CELL_THREADS * kCoopCells >= c->N) {
+        cudaMemsetAsync(c->d_ctr, 0, sizeof(unsigned long long), c->s);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)blocks);
+        cfg.blockDim = dim3(PF_CELL_THREADS);
+        cfg.stream = c->s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_bwd_diffuse_all<R, kCoopCells>, P, DS, C0, Csub, c->l_C, c->l_C2,
+                           c->l_ph, c->d_acc + 3, c->d_ctr, c->d_err, kCoopTimeoutNs, gat_gid, (const int *)c->pub_id,
+                           (const R *)c->pub_l, gat_lphi);
+        if (c->n_sub & 1) std::swap(c->l_C, c->l_C2);
+        return;
+    }
+    const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
+    if (gat_gid) k_bwd_phase_gather<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, gat_gid, c->pub_id, c->pub_l, gat_lphi);
+    for (int k = c->n_sub - 1; k >= 0; k--) {
+        const R *cin = k == 0 ? C0 : Csub + (size_t)(k - 1) * N;
+        k_bwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, DS, cin, c->l_C, c->l_C2, c->l_ph, c->d_acc + 3);
+        std::swap(c->l_C, c->l_C2);
+    }
+}
+
 template <typename R>
 static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     auto *c = new AdjCtx<R>();
@@ -633,13 +836,26 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     const size_t N = (size_t)c->N;
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
-    ok = ok && c->alloc(&c->dscr, 18 * N);
+    ok = ok && c->alloc(&c->dscr, 9 * N);
     ok = ok && c->alloc(&c->v_gid, N) && c->alloc(&c->v_phi, 4 * N) && c->alloc(&c->v_ph, 3 * N) && c->alloc(&c->v_C, N);
     ok = ok && c->alloc(&c->w_gid, N) && c->alloc(&c->w_phi, 4 * N) && c->alloc(&c->w_ph, 3 * N) &&
          c->alloc(&c->w_C, N) && c->alloc(&c->w_C2, N);
     ok = ok && c->alloc(&c->l_phi, 4 * N) && c->alloc(&c->l_ph, 3 * N) && c->alloc(&c->l_C, N) &&
          c->alloc(&c->l_phi2, 4 * N) && c->alloc(&c->l_ph2, 3 * N) && c->alloc(&c->l_C2, N);
     ok = ok && c->alloc(&c->pub_id, LMAX * N) && c->alloc(&c->pub_l, LMAX * N) && c->alloc(&c->d_acc, 8);
+    ok = ok && c->alloc(&c->d_ctr, 1) && c->alloc(&c->d_err, 1);
+    if (ok) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_diffuse_all<R, kCoopCells>, PF_CELL_THREADS,
+                                                          0) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 0;
+        }
+        c->coop_blocks = per_sm * sms;
+        cudaMemsetAsync(c->d_err, 0, sizeof(int), c->s);
+    }
     if (!ok) {
         cudaGetLastError();
         delete c;
@@ -748,7 +964,7 @@ static int ensure_ck(AdjCtx<R> *c, size_t nck, size_t nseg) {
     while (c->sg_gid.size() < nseg) {
         ushort4 *g; R *p, *h, *C, *Cs;
         if (!c->alloc(&g, N) || !c->alloc(&p, 4 * N) || !c->alloc(&h, 3 * N) || !c->alloc(&C, N) ||
-            !c->alloc(&Cs, (size_t)c->n_sub * 9 * N)) {
+            !c->alloc(&Cs, AdjCtx<R>::record_size(c->n_sub, N))) {
             cudaGetLastError();
             return pf_fail(PF_ERR_NOMEM, "adjoint segment allocation failed");
         }
@@ -884,31 +1100,30 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
         return PF_OK;
     };
     auto reverse = [&](int t0, int t1) {
+        // The neighbour part of each reverse phase sweep runs inside the next
+        // reverse diffusion launch (pending), the segment's last one alone.
+        const ushort4 *pend_gid = nullptr;
+        R *pend_lphi = nullptr;
         for (int t = t1 - 1; t >= t0; t--) {
             const int i = t - t0;
-            // Post-sweep phase fractions of step t: the diffusion leaves them
-            // alone, so they are the next step's stored pre-step values (or the
-            // segment's end state for its last step).
-            const R *ph_post = (t + 1 < t1) ? c->sg_ph[i + 1] : c->w_ph;
-            // Reverse the diffusion sub-steps.
-            for (int k = c->n_sub - 1; k >= 0; k--) {
-                const R *ds = c->sg_Csub[i] + (size_t)k * 9 * N;
-                k_bwd_diffuse_d<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, ph_post, ds, ds + 3 * N, ds + 6 * N, c->l_C, c->l_C2, c->l_ph,
-                                                        c->d_acc + 3);
-                std::swap(c->l_C, c->l_C2);
-            }
-            // Reverse the phase sweep.
+            // Reverse the diffusion sub-steps (the step's record holds what
+            // they need of the post-sweep phase fractions).
+            bwd_diffusion(c, P, c->sg_Csub[i], c->sg_C[i], pend_gid, pend_lphi);
+            // Reverse the phase sweep, own part.
             k_bwd_phase_own<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
                                                     c->l_ph, c->l_C, c->l_phi2, c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
-            k_bwd_phase_gather<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->sg_gid[i], c->pub_id, c->pub_l, c->l_phi2);
+            pend_gid = c->sg_gid[i];
+            pend_lphi = c->l_phi2;
             std::swap(c->l_phi, c->l_phi2);
             std::swap(c->l_ph, c->l_ph2);
         }
+        if (pend_gid)
+            k_bwd_phase_gather<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, pend_gid, c->pub_id, c->pub_l, pend_lphi);
     };
     for (int sg = nseg - 1; sg >= 0; sg--) {
         const int t0 = sg * c->K, t1 = std::min(c->nsteps, t0 + c->K);
         // Recompute the segment from its checkpoint, storing every pre-step
-        // state and every sub-step's derived planes, then sweep it backwards.
+        // state and every sub-step's carbon, then sweep it backwards.
         copy_state(c, c->ck_gid[sg], c->ck_phi[sg], c->ck_ph[sg], c->ck_C[sg], c->sg_gid[0], c->sg_phi[0], c->sg_ph[0],
                    c->sg_C[0]);
         if (!seeded || t1 - t0 != c->K) {
@@ -966,9 +1181,16 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
         if (cudaGraphLaunch(c->seg_graph, c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
     }
     double h[8];
+    int herr = 0;
     cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->s);
     cudaEventRecord(e1, c->s);
     if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_gradient failed");
+    if (herr) {
+        cudaMemsetAsync(c->d_err, 0, sizeof(int), c->s);
+        cudaStreamSynchronize(c->s);
+        return pf_fail(PF_ERR_TIMEOUT, "pf_adj_gradient: a grid barrier of the reverse diffusion timed out");
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0); cudaEventDestroy(e1);
