@@ -512,6 +512,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned)
 
 
+def _diffusion_kernel(tuned):
+    """Name of the FP32 diffusion kernel the timed steps launched."""
+    if not tuned:
+        return "k_diffuse_tma (library default where the grid allows TMA, else k_diffuse)"
+    return "k_diffuse_tma" if tuned.get("variant") == 1 else "k_diffuse"
+
+
 def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned=None):
     if rank != 0:
         return None
@@ -541,8 +548,8 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
 
     ms_step = ms / args.steps
     # DRAM traffic of the diffusion kernel: bytes per cell from the committed ncu
-    # capture of a 256x256x64 case (profiles/ncu_traffic.json), scaled to this
-    # launch by its cell count.
+    # capture of a smaller box of the same workload (profiles/ncu_traffic.json),
+    # scaled to this launch by its cell count.
     traffic, traffic_src = None, None
     tpath = os.path.join(REPO, "profiles", "ncu_traffic.json")
     if os.path.exists(tpath):
@@ -559,7 +566,7 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
         "config": _config(wl, grid, P.n_sub, nsol),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": ach / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
-                     "kernel": "k_diffuse_f32",
+                     "kernel": _diffusion_kernel(tuned),
                      "algorithmic_bytes_per_launch": diff_bytes, "mean_launch_ms": t_diff * 1e3,
                      "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)"},
         "kernels": {

@@ -923,11 +923,13 @@ int flux_phases(const pf_f32_params &P) {
 pf_diff_cfg pf_diffuse_default_cfg(const pf_f32_params &P) {
     pf_diff_cfg c;
     c.ty = 16;
-    c.variant = 0;
+    // The TMA-staged variant where the grid allows it (the autotuner's usual
+    // pick on GB300), else plain loads.
+    c.variant = tma_ok(P, 16) ? 1 : 0;
     const int tiles = ((P.ix + kBX - 1) / kBX) * ((P.iy + 15) / 16);
-    // About two waves of 2 resident blocks on 152 SMs, at least 8 planes per block.
+    // About 1024 blocks (several waves on 152 SMs), at least 8 planes per block.
     int z = P.iz;
-    while (z > 8 && (long long)tiles * ((P.iz + z - 1) / z) < 152 * 2 * 2) z = (z + 1) / 2;
+    while (z > 8 && (long long)tiles * ((P.iz + z - 1) / z) < 1024) z = (z + 1) / 2;
     c.zchunk = z < 1 ? 1 : z;
     return c;
 }
