@@ -138,6 +138,8 @@ struct pf_ctx {
     pf_f32_map map{};
     int *d_span = nullptr;
     unsigned int *d_trunc = nullptr;
+    unsigned int *rest = nullptr;        // phase sweep: cells with more than four stencil grains
+    unsigned int *rest_count = nullptr;
     long long truncated = 0;
     // Reference-layout (FP64) staging buffers of the FP32C upload/download,
     // allocated on first use and kept until pf_destroy, so repeated uploads
@@ -218,7 +220,7 @@ void free_all(pf_ctx *c) {
         cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
     }
     cudaFree(c->phase); cudaFree(c->C); cudaFree(c->phase32);
-    cudaFree(c->d_span); cudaFree(c->d_trunc);
+    cudaFree(c->d_span); cudaFree(c->d_trunc); cudaFree(c->rest); cudaFree(c->rest_count);
     cudaFree(c->st_ids); cudaFree(c->st_phi); cudaFree(c->st_phase); cudaFree(c->st_C); cudaFree(c->st_conc);
     cudaFree(c->partials); cudaFree(c->d_red);
     if (c->h_red) cudaFreeHost(c->h_red);
@@ -255,7 +257,7 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         const int a = c->cur;
         e = timed(c, 0, [&] {
             return pf_launch_phase_f32(F, c->gid[a], c->phi32[a], c->gid[1 - a], c->phi32[1 - a], c->phase32,
-                                       c->sol[c->curs], c->stream);
+                                       c->sol[c->curs], c->rest, c->rest_count, c->stream);
         });
         if (e != cudaSuccess) return e;
         c->cur = 1 - a;
@@ -307,6 +309,8 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
     if (precision != PF_PREC_FP64 && precision != PF_PREC_FP32C) return pf_fail(PF_ERR_ARG, "pf_create: bad precision");
     if (model->ix < 1 || model->iy < 1 || model->iz < 1 || model->nsol < 1 || model->nsol > 2 || model->nT < 1)
         return pf_fail(PF_ERR_ARG, "pf_create: bad model");
+    if (precision == PF_PREC_FP32C && (long long)model->ix * model->iy * model->iz > 0xffffffffLL)
+        return pf_fail(PF_ERR_RANGE, "pf_create: the compact FP32 path indexes cells with 32 bits");
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
         cudaGetLastError();
@@ -342,6 +346,8 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         alloc((void **)&c->phase32, 3 * N * sizeof(float));
         alloc((void **)&c->d_span, 8 * sizeof(int));
         alloc((void **)&c->d_trunc, sizeof(unsigned int));
+        alloc((void **)&c->rest, N * sizeof(unsigned int));
+        alloc((void **)&c->rest_count, sizeof(unsigned int));
     }
     c->red_blocks = pf_reduce_blocks(c->N);
     alloc((void **)&c->partials, (size_t)c->red_blocks * PF_RED_NOUT * sizeof(double));

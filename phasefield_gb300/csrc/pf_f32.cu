@@ -19,28 +19,75 @@ constexpr int kPX = 32, kPY = 8, kPT = kPX * kPY;  // phase-sweep block: 32 x 8 
 static_assert(kPX == 32, "one warp per tile row");
 
 // Phase sweep, one thread per cell, 2D blocks of 32x8 cells of one plane (x-y
-// neighbours mostly in the same block's L1 footprint).  Bulk cells (one grain
-// everywhere in the stencil) are copied after a test on the grain ids alone;
-// the merged stencil list of every other cell lives in shared memory columns
-// [entry][thread], so the merge, the pair loop and the top-4 selection run
-// over the list's actual length.  (Measured on GB300: compacting interface
-// cells into a per-tile queue, marching the tile up z with lists in local
-// memory, or matching the cell's own grains in registers all ran 10-17%
-// slower than this form.)
-template <int NSOL>
-__global__ void __launch_bounds__(kPT) k_phase_f32(const __grid_constant__ pf_f32_params P,
-                                                   const ushort4 *__restrict__ gid1,
-                                                   const float4 *__restrict__ phi1,
-                                                   ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
-                                                   float *__restrict__ sphase,
-                                                   const float2 *__restrict__ sol) {
-    __shared__ pf_plist<kPT> L;
-    const int t = threadIdx.x + kPX * threadIdx.y;
+// neighbours mostly in the same block's L1 footprint).  Every cell whose
+// merged stencil list fits four entries is updated with the list in
+// registers (pf_phase_cell_reg); the few others are appended to a work list
+// (one atomic per warp) and updated by k_phase_f32_rest with the ten-entry
+// shared-memory list of pf_phase_cell.  The sweep reads buffer 1 and writes
+// buffer 2 only, so deferring a cell changes nothing it reads.
+__device__ __forceinline__ void pf_defer(bool defer, unsigned n, unsigned int *rest, unsigned int *rest_count) {
+    const unsigned m = __ballot_sync(0xffffffffu, defer);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        unsigned base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(rest_count, (unsigned)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+        if (defer) rest[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)n;
+    }
+}
+
+// Four resident blocks per SM (64 registers): measured faster than three
+// (75 registers, no spills) or five and six (heavy spills).
+template <int NSOL, int MINB>
+__global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__ pf_f32_params P,
+                                                         const ushort4 *__restrict__ gid1,
+                                                         const float4 *__restrict__ phi1,
+                                                         ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
+                                                         float *__restrict__ sphase,
+                                                         const float2 *__restrict__ sol,
+                                                         unsigned int *__restrict__ rest,
+                                                         unsigned int *__restrict__ rest_count) {
+    const int ix = P.ix, iy = P.iy, iz = P.iz;
     const int i = blockIdx.x * kPX + threadIdx.x;
     const int j = blockIdx.y * kPY + threadIdx.y;
     const int k = blockIdx.z;
-    if (i >= P.ix || j >= P.iy) return;
-    pf_phase_cell<NSOL, kPT>(P, i, j, k, t, gid1, phi1, gid2, phi2, sphase, sol, L);
+    const unsigned plane = (unsigned)ix * (unsigned)iy;
+    const unsigned n = (unsigned)i + (unsigned)ix * (unsigned)j + plane * (unsigned)k;
+    bool defer = false;
+    if (i < ix && j < iy) {
+        unsigned nb[6];
+        nb[0] = n - i + pf_wrap(i, ix, -1);
+        nb[1] = n - i + pf_wrap(i, ix, 1);
+        nb[2] = n + (unsigned)ix * (pf_wrap(j, iy, -1) - j);
+        nb[3] = n + (unsigned)ix * (pf_wrap(j, iy, 1) - j);
+        nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
+        nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
+        defer = !pf_phase_cell_reg<NSOL>(P, n, nb, gid1, phi1, gid2, phi2, sphase, sol);
+    }
+    // One row of the block is one warp: every lane reaches the vote.
+    pf_defer(defer, n, rest, rest_count);
+}
+
+// The deferred cells of k_phase_f32, one per thread, with the general
+// ten-entry list (solver.cpp:147-304 without the four-entry limit).
+template <int NSOL>
+__global__ void __launch_bounds__(kPT) k_phase_f32_rest(const __grid_constant__ pf_f32_params P,
+                                                        const ushort4 *__restrict__ gid1,
+                                                        const float4 *__restrict__ phi1,
+                                                        ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
+                                                        float *__restrict__ sphase,
+                                                        const float2 *__restrict__ sol,
+                                                        const unsigned int *__restrict__ rest,
+                                                        const unsigned int *__restrict__ rest_count) {
+    __shared__ pf_plist<kPT> L;
+    const unsigned cnt = *rest_count;
+    const unsigned ix = (unsigned)P.ix, iy = (unsigned)P.iy;
+    for (unsigned q = blockIdx.x * kPT + threadIdx.x; q < cnt; q += gridDim.x * kPT) {
+        const unsigned n = rest[q];
+        const unsigned r = n / ix;
+        pf_phase_cell<NSOL, kPT>(P, (int)(n - r * ix), (int)(r % iy), (int)(r / iy), threadIdx.x, gid1, phi1,
+                                 gid2, phi2, sphase, sol, L);
+    }
 }
 
 // Per-class maximum of (id mod 100000) over all slots, for the local id map.
@@ -248,12 +295,20 @@ cudaError_t pf_launch_unpack_f32(const pf_step_params &P, const pf_f32_map &map,
 
 cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, const float4 *phi1,
                                 ushort4 *gid2, float4 *phi2, float *sphase, const float2 *sol,
-                                cudaStream_t s) {
+                                unsigned int *rest, unsigned int *rest_count, cudaStream_t s) {
     const dim3 block(kPX, kPY);
     const dim3 grid((unsigned)((P.ix + kPX - 1) / kPX), (unsigned)((P.iy + kPY - 1) / kPY), (unsigned)P.iz);
-    if (P.nsol == 2)
-        k_phase_f32<2><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol);
-    else
-        k_phase_f32<1><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol);
+    long long rb = (P.N / 64 + kPT - 1) / kPT;  // the rest kernel loops if more than 1/64 of the cells wait
+    if (rb > 152 * 5) rb = 152 * 5;
+    if (rb < 1) rb = 1;
+    cudaError_t e = cudaMemsetAsync(rest_count, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    if (P.nsol == 2) {
+        k_phase_f32<2, 4><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        k_phase_f32_rest<2><<<(unsigned)rb, kPT, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+    } else {
+        k_phase_f32<1, 4><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        k_phase_f32_rest<1><<<(unsigned)rb, kPT, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+    }
     return cudaGetLastError();
 }

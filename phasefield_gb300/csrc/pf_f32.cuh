@@ -226,3 +226,194 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     sphase[N + n] = sqrtf(ph[1] * inv);
     sphase[2 * N + n] = sqrtf(ph[2] * inv);
 }
+
+// The same update for a cell whose merged stencil list has at most four
+// grains -- about 98% of the cells of 3D Voronoi/nucleus microstructures --
+// with the list held in registers: the merge compares each neighbour slot
+// with the four entries at once, the pair loop, the clamps and the top-four
+// selection are unrolled over the four entries with the list length as a
+// predicate, so the lanes of a warp stay together.  The entry order, the
+// summation order of every pair term and the selection rule are those of
+// pf_phase_cell, so both routes give the same values for such a cell.
+// Returns false, having written nothing, for a cell the register list cannot
+// hold (a fifth grain in the stencil, or own slots above the cutoff that are
+// not a prefix); the caller routes that cell to pf_phase_cell.  Cell indices
+// are 32-bit (grids of fewer than 2^32 cells).
+template <int NSOL, bool CG = false>
+__device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsigned n, const unsigned nb[6],
+                                                  const ushort4 *__restrict__ gid1,
+                                                  const float4 *__restrict__ phi1, ushort4 *__restrict__ gid2,
+                                                  float4 *__restrict__ phi2, float *__restrict__ sphase,
+                                                  const float2 *__restrict__ sol) {
+    const float cutoff = P.cutoff;
+    const int b1 = P.b1, b2 = P.b2, nnb = P.nnb;
+    const ushort4 g = pf_ld<CG>(gid1 + n);
+    const float4 v = pf_ld<CG>(phi1 + n);
+    ushort4 ng[6];
+    float4 nv[6];
+#pragma unroll
+    for (int b = 0; b < 6; b++) {
+        if (b < nnb) {
+            ng[b] = pf_ld<CG>(gid1 + nb[b]);
+            nv[b] = pf_ld<CG>(phi1 + nb[b]);
+        } else {
+            ng[b] = make_ushort4(0, 0, 0, 0);
+            nv[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    // Bulk cell: one grain here and the same single grain in every neighbour.
+    if (g.y == 0 && g.z == 0 && g.w == 0 && v.x > cutoff) {
+        bool bulk = true;
+#pragma unroll
+        for (int b = 0; b < 6; b++)
+            if (b < nnb) bulk = bulk && ng[b].x == g.x && ng[b].y == 0;
+        if (bulk) {
+            gid2[n] = g;
+            phi2[n] = v;
+            return true;
+        }
+    }
+    // solver.cpp:168-177: own slots above the cutoff, in slot order.
+    const bool ok0 = v.x > cutoff, ok1 = v.y > cutoff, ok2 = v.z > cutoff, ok3 = v.w > cutoff;
+    if ((ok1 && !ok0) || (ok2 && !ok1) || (ok3 && !ok2)) return false;
+    int lid[4] = {ok0 ? (int)g.x : 0, ok1 ? (int)g.y : 0, ok2 ? (int)g.z : 0, ok3 ? (int)g.w : 0};
+    float v1[4] = {ok0 ? v.x : 0.f, ok1 ? v.y : 0.f, ok2 ? v.z : 0.f, ok3 ? v.w : 0.f};
+    float v2[4] = {0.f, 0.f, 0.f, 0.f};
+    int num = (int)ok0 + (int)ok1 + (int)ok2 + (int)ok3;
+    // solver.cpp:179-205: neighbours x-, x+, y-, y+, z-, z+, each scanned to
+    // its first empty slot; an id already listed adds its value, a new id is
+    // appended.  Entries past num hold id 0, which no live slot carries.
+    bool full = false;
+#pragma unroll
+    for (int b = 0; b < 6; b++) {
+        if (b < nnb) {
+            const int nid[4] = {ng[b].x, ng[b].y, ng[b].z, ng[b].w};
+            const float nvv[4] = {nv[b].x, nv[b].y, nv[b].z, nv[b].w};
+            bool live = true;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int tid = nid[a];
+                live = live && tid != 0;
+                if (live) {
+                    const float tv = nvv[a];
+                    bool hit = false;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const bool m = lid[e] == tid;
+                        if (m) v2[e] += tv;
+                        hit = hit || m;
+                    }
+                    if (!hit) {
+                        if (num < 4) {
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                                if (e == num) {
+                                    lid[e] = tid;
+                                    v2[e] = tv;
+                                }
+                            num++;
+                        } else {
+                            full = true;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (full) return false;
+    if (num == 1) {  // solver.cpp:207-216
+        gid2[n] = g;
+        phi2[n] = v;
+        return true;
+    }
+    float ph_old[3] = {0.f, 0.f, 0.f};
+    {
+        const int oid[4] = {g.x, g.y, g.z, g.w};
+        const float ov[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const int p = pf_lphase(oid[a], b1, b2);
+            if (p == 1) ph_old[0] += ov[a];
+            else if (p == 2) ph_old[1] += ov[a];
+            else if (p == 3) ph_old[2] += ov[a];
+        }
+    }
+    float lc[3];
+    pf_partition_q(P, 0, pf_ld<CG>(sol + n * NSOL).x, ph_old, lc);
+    int pe[4];
+    float ce[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        pe[e] = pf_lphase(lid[e], b1, b2);
+        ce[e] = pe[e] == 1 ? lc[0] : (pe[e] == 2 ? lc[1] : lc[2]);
+    }
+    // Pair terms, each unordered pair once, in the order of pf_phase_cell.
+    float del[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        if (a < num) {
+            float da = del[a];
+#pragma unroll
+            for (int b = a + 1; b < 4; b++) {
+                if (b < num) {
+                    const int e = (pe[a] - 1) + 3 * (pe[b] - 1), ee = (pe[b] - 1) + 3 * (pe[a] - 1);
+                    const float X = v2[a] * v1[b] - v2[b] * v1[a];
+                    const float Y = v1[a] - v1[b];
+                    const float Z = sqrtf(v1[a] * v1[b]);
+                    const float sym = P.A[e] * X + P.B[e] * Y;
+                    da += sym + P.G[e] * Z * (ce[a] - P.E[e]);
+                    del[b] += -sym + P.G[ee] * Z * (ce[b] - P.E[ee]);
+                }
+            }
+            float d = v1[a] + da;
+            if (d > 1.0f) d = 1.0f;
+            else if (d < cutoff) d = 0.f;
+            del[a] = d;
+        }
+    }
+    // Top four, first maximum wins, the maximum swapped into place.
+    float ph[3] = {0.f, 0.f, 0.f};
+    float sum = 0.f;
+    int kid[4];
+    float kv[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        kid[a] = 0;
+        kv[a] = 0.f;
+        if (a < num) {
+            int mx = a, mid = lid[a];
+            float mv = del[a];
+#pragma unroll
+            for (int b = a + 1; b < 4; b++)
+                if (b < num && del[b] > mv) {
+                    mv = del[b];
+                    mx = b;
+                    mid = lid[b];
+                }
+#pragma unroll
+            for (int b = a + 1; b < 4; b++)
+                if (b == mx) {
+                    del[b] = del[a];
+                    lid[b] = lid[a];
+                }
+            if (mv > cutoff) {
+                kid[a] = mid;
+                kv[a] = mv;
+                const int p = pf_lphase(mid, b1, b2);
+                if (p == 1) ph[0] += mv;
+                else if (p == 2) ph[1] += mv;
+                else ph[2] += mv;
+                sum += mv;
+            }
+        }
+    }
+    const float inv = 1.f / sum;
+    gid2[n] = make_ushort4((unsigned short)kid[0], (unsigned short)kid[1], (unsigned short)kid[2],
+                           (unsigned short)kid[3]);
+    phi2[n] = make_float4(kv[0] * inv, kv[1] * inv, kv[2] * inv, kv[3] * inv);
+    const long long N = P.N;
+    sphase[n] = sqrtf(ph[0] * inv);
+    sphase[N + n] = sqrtf(ph[1] * inv);
+    sphase[2 * N + n] = sqrtf(ph[2] * inv);
+    return true;
+}

@@ -29,9 +29,11 @@ cudaError_t pf_launch_unpack_f32(const pf_step_params &P, const pf_f32_map &map,
                                  const float4 *phi, const float *phase, const float2 *sol, int *ids64,
                                  double *phi64, double *phase64, double *conc64, double *C64,
                                  cudaStream_t s);
+// 'rest' holds N cell indices and 'rest_count' one counter: the cells whose
+// stencil list exceeds four entries wait there between the sweep's two kernels.
 cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, const float4 *phi1,
                                 ushort4 *gid2, float4 *phi2, float *phase, const float2 *sol,
-                                cudaStream_t s);
+                                unsigned int *rest, unsigned int *rest_count, cudaStream_t s);
 // Tile shape of the diffusion kernel: TX = 32 cells in x, ty in y, zchunk z
 // planes per block, kernel variant (chosen by the autotuner or the default rule).
 struct pf_diff_cfg {
