@@ -284,6 +284,31 @@ int pf_write_data(pf_ctx *ctx, const char *directory, int forced, int *written);
 int pf_write_vti(const char *path, int ix, int iy, int iz, double dx, const int32_t *ids,
                  const double *C);
 
+/* The seeded initial state of 'spec' at 'time' generated on the device,
+ * straight into the context (replaces pf_init_microstructure + upload; no
+ * host arrays).  The same generator code as pf_init_microstructure, run one
+ * cell per thread: the grain ids and solutes equal the host's, the phase
+ * values agree to a few ulp (the device's tanh).  PF_ERR_RANGE if more than
+ * 256 nuclei or particles lie near one cell. */
+int pf_init_device(pf_ctx *ctx, const pf_init_spec *spec, double time);
+
+/* Microstructure files in appended raw binary VTK image data, written from
+ * the device state while stepping continues (the MPI variant's piece files and
+ * .pvti index, C++-MPI/source/write_data.cpp:30-110, with the fields of
+ * write_data.cpp:42-82: Int32 "korn" = 0 where the second slot is occupied,
+ * else the phase of the first grain; Float32 "conc" = total carbon).  The
+ * fields are formed by a kernel on the context's stream, copied to pinned
+ * memory on a stream of their own and written by a host thread as 'pieces'
+ * z slabs (neighbours share a plane) named <index:07d>_<piece>.vti, plus
+ * <index:07d>.pvti.  Returns once the kernel is enqueued; a later call (or
+ * pf_write_wait) first waits for the write in flight.  pf_write_wait returns
+ * that write's status. */
+int pf_write_vti_binary(pf_ctx *ctx, const char *directory, int index, int pieces);
+int pf_write_wait(pf_ctx *ctx);
+/* The same files from host arrays korn[N], conc[N] (synchronous). */
+int pf_write_vti_binary_host(const char *directory, int index, int pieces, int ix, int iy, int iz, double dx,
+                             const int32_t *korn, const float *conc);
+
 /* No counterpart in the reference.  The statistics of pf_reduce (same 8
  * outputs, written to the device array d_out) for caller-owned device arrays in
  * the reference layout, computed without allocating anything: for callers that

@@ -146,6 +146,10 @@ SYMBOLS = {
     "pf_write_data": (_I, [_P, ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
     "pf_write_vti": (_I, [ctypes.c_char_p, _I, _I, _I, _D, _P, _P]),
     "pf_reduce_noalloc": (_I, [ctypes.c_longlong, _I, _P, _P, _P, _P, _P, _P]),
+    "pf_write_vti_binary": (_I, [_P, ctypes.c_char_p, _I, _I]),
+    "pf_write_wait": (_I, [_P]),
+    "pf_init_device": (_I, [_P, _P, _D]),
+    "pf_write_vti_binary_host": (_I, [ctypes.c_char_p, _I, _I, _I, _I, _I, _D, _P, _P]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfModel), _I, ctypes.POINTER(_P)]),
     "pf_batch_upload": (_I, [_P, _I, _P, _P, _P, _P, _D]),
     "pf_batch_run": (_I, [_P, _I]),
@@ -279,6 +283,12 @@ class PhaseField:
         check(lib().pf_upload_state(self._ctx, _ptr(state["ids"]), _ptr(state["phi"]), _ptr(state["phase"]),
                                     _ptr(state.get("conc")), _ptr(state["C"]), time), "pf_upload_state")
 
+    def construct_on_device(self, spec: PfInitSpec, time: float | None = None) -> None:
+        """The seeded initial state generated on the GPU, straight into the
+        context (pf_init_device): no host arrays, no upload."""
+        t = self.model.T_time[0] if time is None else time
+        check(lib().pf_init_device(self._ctx, ctypes.byref(spec), t), "pf_init_device")
+
     def construct(self, spec: PfInitSpec, time: float | None = None) -> dict:
         """Seeded replacement of Construct + Nucleate1in2; uploads and returns the state."""
         t = self.model.T_time[0] if time is None else time
@@ -377,6 +387,14 @@ class PhaseField:
         n = (ctypes.c_longlong * 2)()
         check(lib().pf_kernel_times(self._ctx, t, n), "pf_kernel_times")
         return {"phase": (t[0], n[0]), "diffusion": (t[1], n[1])}
+
+    def write_vti_binary(self, directory: str, index: int, pieces: int = 1) -> None:
+        """Binary microstructure files of the current state, written by a host
+        thread from device buffers while stepping continues (pf_write_vti_binary)."""
+        check(lib().pf_write_vti_binary(self._ctx, directory.encode(), index, pieces), "pf_write_vti_binary")
+
+    def write_wait(self) -> None:
+        check(lib().pf_write_wait(self._ctx), "pf_write_wait")
 
     def write_data(self, directory: str | None = None, forced: bool = False) -> bool:  # noqa: D401
         """phase_field::Write_data (write_data.cpp:3-40)."""

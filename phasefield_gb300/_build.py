@@ -6,6 +6,8 @@ Each translation unit is compiled in parallel with its own flags:
   multiply-adds, so they reproduce the CPU solver's rounding exactly.
 * ``pf_f32.cu``  ``-prec-div=false -prec-sqrt=false``: approximate division and
   square root in the FP32 kernels (the solute update is compensated).
+* ``pf_f32_diffuse.cu`` additionally ``-fmad=false``: every kernel variant of the
+  diffusion sub-step rounds identically (their FMAs are explicit).
 * ``pf_host.cpp`` ``-ffp-contract=off``: host-side per-step parameters must be
   bit-identical to the reference's host arithmetic on x86 and on Arm.
 
@@ -46,17 +48,22 @@ NVCC_FLAGS = ARCH + [
 PER_FILE = {
     "pf_f64.cu": ["-fmad=false"],
     "pf_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
-    "pf_f32_diffuse.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    # no implicit contraction: every variant of the sub-step kernel must round
+    # identically (every intended FMA is an explicit fmaf)
+    "pf_f32_diffuse.cu": ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"],
     "pf_batch.cu": ["-prec-div=false", "-prec-sqrt=false"],
     # no implicit contraction (forward and reverse must rebuild identical
     # decisions); approximate FP32 division/sqrt (same code path in both)
     "pf_adjoint.cu": ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"],
+    # the device generator rounds as the host generator does
+    "pf_init_dev.cu": ["-fmad=false"],
 }
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
              "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["pf_f64.cu", "pf_f32.cu", "pf_f32_diffuse.cu", "pf_batch.cu", "pf_reduce.cu", "pf_api.cu",
-              "pf_reduce_noalloc.cu", "pf_adjoint.cu"]
+              "pf_reduce_noalloc.cu", "pf_adjoint.cu", "pf_output.cu",
+              "pf_init_dev.cu"]
 CXX_SOURCES = ["pf_host.cpp", "pf_init.cpp"]
 HEADERS = ["pf_types.h", "pf_dev.cuh", "pf_f32.cuh", "pf_kernels.h", "pf_host.h", "pf_init.h"]
 

@@ -16,6 +16,7 @@
 #include "pf_dev.cuh"
 #include "pf_host.h"
 #include "pf_kernels.h"
+#include "pf_output.h"
 
 static int pf_cuda_fail(cudaError_t e) {
     return pf_fail(PF_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
@@ -140,6 +141,7 @@ struct pf_ctx {
     unsigned int *d_trunc = nullptr;
     unsigned int *rest = nullptr;        // phase sweep: cells with more than four stencil grains
     unsigned int *rest_count = nullptr;
+    pf_out *out = nullptr;               // asynchronous binary microstructure writer
     long long truncated = 0;
     // Reference-layout (FP64) staging buffers of the FP32C upload/download,
     // allocated on first use and kept until pf_destroy, so repeated uploads
@@ -215,6 +217,8 @@ cudaError_t timed(pf_ctx *c, int kind, F launch) {
 }
 
 void free_all(pf_ctx *c) {
+    pf_out_destroy(c->out);
+    c->out = nullptr;
     for (int i = 0; i < 2; i++) {
         cudaFree(c->ids[i]); cudaFree(c->phi[i]); cudaFree(c->conc[i]);
         cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
@@ -301,6 +305,41 @@ bool same_step(const pf_step_params &a, const pf_step_params &b) {
 // Buffer-role signature: graphs are captured for a fixed assignment.
 int role_sig(const pf_ctx *c) { return c->cur | (c->curc << 1) | (c->curs << 2); }
 
+}  // namespace
+
+namespace {
+// The reference-layout state in the FP32C context's staging buffers -> the
+// compact layout: local id map from the grain-id spans, then the pack kernel.
+int pack_staged(pf_ctx *c, const char *who) {
+    int st = PF_OK;
+    cudaMemsetAsync(c->d_span, 0, 8 * sizeof(int), c->stream);
+    cudaMemsetAsync(c->d_trunc, 0, sizeof(unsigned int), c->stream);
+    pf_launch_id_span(c->st_ids, c->N, c->d_span, c->stream);
+    int span[8];
+    cudaError_t e = cudaMemcpyAsync(span, c->d_span, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) st = pf_cuda_fail(e);
+    else if (span[4] != 0) st = pf_fail(PF_ERR_RANGE, std::string(who) + ": grain id outside 0..399999");
+    else {
+        c->map.off[0] = 0;
+        c->map.off[1] = span[0];
+        c->map.off[2] = span[0] + span[1];
+        c->map.off[3] = span[0] + span[1] + span[2];
+        c->map.total = c->map.off[3] + span[3];
+        if (c->map.total > 65535) st = pf_fail(PF_ERR_RANGE, std::string(who) + ": more than 65535 grains");
+    }
+    if (st == PF_OK) {
+        e = pf_launch_pack_f32(c->N, c->nsol, c->map, c->st_ids, c->st_phi, c->st_phase, c->st_C, c->gid[0],
+                               c->phi32[0], c->phase32, c->sol[0], c->d_trunc, c->stream);
+        unsigned int tr = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&tr, c->d_trunc, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) st = pf_cuda_fail(e);
+        c->truncated = tr;
+    }
+    cudaStreamSynchronize(c->stream);
+    return st;
+}
 }  // namespace
 
 extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
@@ -408,44 +447,12 @@ extern "C" int pf_upload_state(pf_ctx *c, const int32_t *ids, const double *phi,
     } else {
         // The reference layout is staged in the context's FP64 buffers and
         // packed on the device.
-        int st = PF_OK;
-        if (!ensure_staging(c, false)) st = pf_fail(PF_ERR_NOMEM, "pf_upload_state: staging allocation failed");
-        int *d_ids = c->st_ids;
-        double *d_phi = c->st_phi, *d_phase = c->st_phase, *d_C = c->st_C;
-        cudaError_t e = cudaSuccess;
-        if (st == PF_OK) {
-            cudaMemcpyAsync(d_ids, ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
-            cudaMemcpyAsync(d_phi, phi, 6 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-            cudaMemcpyAsync(d_phase, phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-            cudaMemcpyAsync(d_C, C, N * c->nsol * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-            cudaMemsetAsync(c->d_span, 0, 8 * sizeof(int), c->stream);
-            cudaMemsetAsync(c->d_trunc, 0, sizeof(unsigned int), c->stream);
-            pf_launch_id_span(d_ids, c->N, c->d_span, c->stream);
-            int span[8];
-            e = cudaMemcpyAsync(span, c->d_span, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-            if (e != cudaSuccess) st = pf_cuda_fail(e);
-            else if (span[4] != 0) st = pf_fail(PF_ERR_RANGE, "pf_upload_state: grain id outside 0..399999");
-            else {
-                c->map.off[0] = 0;
-                c->map.off[1] = span[0];
-                c->map.off[2] = span[0] + span[1];
-                c->map.off[3] = span[0] + span[1] + span[2];
-                c->map.total = c->map.off[3] + span[3];
-                if (c->map.total > 65535) st = pf_fail(PF_ERR_RANGE, "pf_upload_state: more than 65535 grains");
-            }
-            if (st == PF_OK) {
-                e = pf_launch_pack_f32(c->N, c->nsol, c->map, d_ids, d_phi, d_phase, d_C, c->gid[0], c->phi32[0],
-                                       c->phase32, c->sol[0], c->d_trunc, c->stream);
-                unsigned int tr = 0;
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(&tr, c->d_trunc, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-                if (e != cudaSuccess) st = pf_cuda_fail(e);
-                c->truncated = tr;
-            }
-        }
-        cudaStreamSynchronize(c->stream);
+        if (!ensure_staging(c, false)) return pf_fail(PF_ERR_NOMEM, "pf_upload_state: staging allocation failed");
+        cudaMemcpyAsync(c->st_ids, ids, 6 * N * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(c->st_phi, phi, 6 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(c->st_phase, phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(c->st_C, C, N * c->nsol * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        const int st = pack_staged(c, "pf_upload_state");
         if (st != PF_OK) return st;
     }
     c->have_state = true;
@@ -1127,5 +1134,57 @@ extern "C" int pf_write_data(pf_ctx *c, const char *directory, int forced, int *
     }
     c->last_temperature_written = temperature;
     if (written) *written = 1;
+    return PF_OK;
+}
+
+// ===========================================================================
+// 4. Binary microstructure files from device buffers (pf_output.cu).
+// ===========================================================================
+extern "C" int pf_write_vti_binary(pf_ctx *c, const char *directory, int index, int pieces) {
+    if (!c || !directory || index < 0 || pieces < 1) return pf_fail(PF_ERR_ARG, "pf_write_vti_binary: bad argument");
+    if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_write_vti_binary: no state uploaded");
+    if (!c->out) c->out = pf_out_create();
+    const pf_model &m = c->model;
+    if (c->prec == PF_PREC_FP64)
+        return pf_out_write_fp64(c->out, c->stream, m.ix, m.iy, m.iz, m.dx, c->ids[c->cur], c->C, directory, index,
+                                 pieces);
+    return pf_out_write_fp32(c->out, c->stream, m.ix, m.iy, m.iz, m.dx, c->nsol, c->map.off[2], c->map.off[3],
+                             c->gid[c->cur], c->sol[c->curs], directory, index, pieces);
+}
+
+extern "C" int pf_write_wait(pf_ctx *c) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_write_wait: null context");
+    return pf_out_wait(c->out);
+}
+
+// ===========================================================================
+// 5. Seeded initial state generated on the device (pf_init_dev.cu).
+// ===========================================================================
+extern "C" int pf_init_device(pf_ctx *c, const pf_init_spec *spec, double time) {
+    if (!c || !spec) return pf_fail(PF_ERR_ARG, "pf_init_device: null argument");
+    const pf_model &m = c->model;
+    pf_step_params P;
+    pf_compute_params(m, time, P);
+    c->time = time;
+    c->cur = c->curc = c->curs = 0;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    const char *msg = nullptr;
+    int st;
+    if (c->prec == PF_PREC_FP64) {
+        st = pf_init_generate_device(m.ix, m.iy, m.iz, c->nsol, m.cutoff, spec, &P.k[0][0], &P.c[0][0], c->ids[0],
+                                     c->phi[0], c->phase, c->conc[0], c->C, c->stream, &msg);
+    } else {
+        if (!ensure_staging(c, false)) return pf_fail(PF_ERR_NOMEM, "pf_init_device: staging allocation failed");
+        st = pf_init_generate_device(m.ix, m.iy, m.iz, c->nsol, m.cutoff, spec, nullptr, nullptr, c->st_ids,
+                                     c->st_phi, c->st_phase, nullptr, c->st_C, c->stream, &msg);
+        if (st == PF_OK) {
+            c->have_state = false;
+            st = pack_staged(c, "pf_init_device");
+            if (st != PF_OK) return st;
+        }
+    }
+    if (st != PF_OK) return pf_fail(st, std::string("pf_init_device: ") + (msg ? msg : "failed"));
+    c->have_state = true;
+    c->have_last = false;
     return PF_OK;
 }

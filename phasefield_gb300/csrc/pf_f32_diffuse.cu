@@ -100,21 +100,24 @@ __device__ __forceinline__ Rec<NPF> derive(const pf_f32_params &P, const float s
     const float ph[3] = {s3[0] * s3[0], s3[1] * s3[1], s3[2] * s3[2]};
 #pragma unroll
     for (int p = 0; p < NPF; p++) R.s[p] = s3[p];
+    // Every sum is written as explicit fused multiply-adds (the file is built
+    // with -fmad=false): no contraction is left to the compiler, so each
+    // kernel variant that derives records rounds them identically.
     if (P.sep[0]) {
-        const float S = ph[0] * P.a[0][0] + ph[1] * P.a[0][1] + ph[2] * P.a[0][2];
+        const float S = fmaf(ph[2], P.a[0][2], fmaf(ph[1], P.a[0][1], ph[0] * P.a[0][0]));
         const float r = __fdividef(C[0], S);
 #pragma unroll
         for (int p = 0; p < NPF; p++) R.c[p] = P.a[0][p] * r;
     } else {
 #pragma unroll
         for (int i = 0; i < NPF; i++) {
-            const float t1 = ph[0] * P.k[0][i] + ph[1] * P.k[0][i + 3] + ph[2] * P.k[0][i + 6];
-            const float t2 = ph[0] * P.c[0][i] + ph[1] * P.c[0][i + 3] + ph[2] * P.c[0][i + 6];
+            const float t1 = fmaf(ph[2], P.k[0][i + 6], fmaf(ph[1], P.k[0][i + 3], ph[0] * P.k[0][i]));
+            const float t2 = fmaf(ph[2], P.c[0][i + 6], fmaf(ph[1], P.c[0][i + 3], ph[0] * P.c[0][i]));
             R.c[i] = __fdividef(C[0] - t2, t1);
         }
     }
     if constexpr (NSOL == 2) {
-        const float S = ph[0] * P.a[1][0] + ph[1] * P.a[1][1] + ph[2] * P.a[1][2];
+        const float S = fmaf(ph[2], P.a[1][2], fmaf(ph[1], P.a[1][1], ph[0] * P.a[1][0]));
         R.r = __fdividef(C[1], S);
     } else {
         R.r = 0.f;
@@ -993,3 +996,4 @@ cudaError_t pf_launch_diffuse_f32(const pf_f32_params &P, const float *sphase, c
     return three ? launch_nnb<1, 3>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk)
                  : launch_nnb<1, 2>(P, sphase, sol_in, sol_out, s, c.ty, c.zchunk);
 }
+

@@ -81,3 +81,8 @@ cudaError_t pf_launch_reduce_f64(long long N, int nsol, const int *ids, const do
 cudaError_t pf_launch_reduce_f32(long long N, int nsol, int deformed_max_local, const ushort4 *gid,
                                  const float4 *phi, const float *phase, const float2 *sol,
                                  double *partials, int nblocks, double *out, cudaStream_t s);
+
+// ---- seeded initial state on the device (pf_init_dev.cu) ----
+int pf_init_generate_device(int ix, int iy, int iz, int nsol, double cutoff, const pf_init_spec *spec,
+                            const double *kq, const double *cq, int32_t *d_ids, double *d_phi, double *d_phase,
+                            double *d_conc, double *d_C, cudaStream_t s, const char **msg);
