@@ -34,6 +34,7 @@ import argparse
 import ctypes
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -399,9 +400,6 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     cfg, m = _model_for(wl, grid)
     spec = wl.spec() if tuple(grid) == tuple(wl.grid) else _scaled_spec(wl, grid)
     spec.seed = wl.seed + rank
-    _log(f"initial state {grid}")
-    st0 = pf.init_microstructure(m, spec, 0.0)
-    _log("initial state done")
     N = grid[0] * grid[1] * grid[2]
     P = pf.params_at(m, 0.0)
     nsol = m.nsol
@@ -422,10 +420,25 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
+    # ---- initial state, generated on the device (pf_init_device) ---------
+    # The reference-layout context also serves the FP64 leg, and its download
+    # is the host state of the e2e leg.
+    _log(f"initial state {grid} on the device")
+    G = pf.PhaseField(m, pf.PF_PREC_FP64)
+    G.set_stream(stream.cuda_stream)
+    G.construct_on_device(spec, 0.0)  # warm-up (module load, first allocations)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    G.construct_on_device(spec, 0.0)
+    torch.cuda.synchronize()
+    init_dev_s = time.perf_counter() - t0
+    st0 = {k: v for k, v in G.download().items() if isinstance(v, np.ndarray)} if not args.no_e2e else None
+    _log("initial state done")
+
     # ---- value: FP32-compensated step, state resident in HBM -------------
     F = pf.PhaseField(m, pf.PF_PREC_FP32C)
     F.set_stream(stream.cuda_stream)
-    F.upload(st0, 0.0)
+    F.construct_on_device(spec, 0.0)
     tuned = F.autotune() if not args.no_tune else None
     F.update(args.warmup)
     F.enable_kernel_timing(True)
@@ -446,6 +459,23 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     value = world * N * args.steps / (ms / 1e3)
     fr_end = F.fractions()
     F.enable_kernel_timing(False)
+    # Binary microstructure files written from the device state while two
+    # more steps run (pf_write_vti_binary): time to enqueue, and until written.
+    out_dir = tempfile.mkdtemp(prefix="pfvti_")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    F.write_vti_binary(out_dir, 0, 16)
+    t_enq = time.perf_counter() - t0
+    F.update(2)
+    torch.cuda.synchronize()
+    t_steps = time.perf_counter() - t0
+    F.write_wait()
+    t_all = time.perf_counter() - t0
+    vti_bytes = sum(os.path.getsize(os.path.join(out_dir, f)) for f in os.listdir(out_dir))
+    shutil.rmtree(out_dir, ignore_errors=True)
+    output = {"pieces": 16, "bytes": vti_bytes, "enqueue_ms": t_enq * 1e3, "two_steps_after_ms": t_steps * 1e3,
+              "written_s": t_all, "note": "fields formed on the device, copied on a side stream and written by "
+                                          "host threads while the two steps ran"}
     F.close()
 
     _log("FP32C leg done")
@@ -453,9 +483,6 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     fp64 = None
     if args.fp64_steps > 0:
         k64 = max(1, min(args.steps, args.fp64_steps))
-        G = pf.PhaseField(m, pf.PF_PREC_FP64)
-        G.set_stream(stream.cuda_stream)
-        G.upload(st0, 0.0)
         G.update(1)
         G.enable_kernel_timing(True)
         torch.cuda.synchronize()
@@ -466,13 +493,17 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         torch.cuda.synchronize()
         ms64 = max_over_ranks(g0.elapsed_time(g1))
         kt64 = G.kernel_times()
-        G.close()
         value64 = world * N * k64 / (ms64 / 1e3)
         fp64 = {"value": value64, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
                 "phase_ms": kt64["phase"][0] / max(1, kt64["phase"][1]),
                 "diffusion_ms": kt64["diffusion"][0] / max(1, kt64["diffusion"][1])}
+    G.close()
+    extra = {"init": {"device_s": init_dev_s, "how": "pf_init_device: the seeded generator run one cell per GPU "
+                                                    "thread into the FP64 reference-layout context"},
+             "output": output}
     if args.no_e2e:
-        return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk, tuned)
+        return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, None, clk, tuned,
+                       extra)
 
     _log("FP64 leg done")
     # ---- e2e: through the C ABI with pinned host buffers -----------------
@@ -511,7 +542,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     e2e = {"value": world * N * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(state_bytes / args.steps),
            "d2h_bytes_per_step": int(64 + down_bytes / args.steps)}
-    return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned)
+    return _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned,
+                   extra)
 
 
 def _diffusion_kernel(tuned):
@@ -521,7 +553,8 @@ def _diffusion_kernel(tuned):
     return "k_diffuse_tma" if tuned.get("variant") == 1 else "k_diffuse"
 
 
-def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned=None):
+def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr_end, fp64, e2e, clk, tuned=None,
+            extra=None):
     if rank != 0:
         return None
     pk = _peaks()
@@ -539,7 +572,14 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import pyoracle as po
 
+        g0 = time.perf_counter()
         om, cst, cells, _, label = cpu_sample(wl, grid)
+        gen_s = time.perf_counter() - g0  # the slab's state from the host generator (plus set-up)
+        if extra is not None and "init" in extra:
+            extra["init"]["host_s_estimate"] = gen_s * grid[2] / (cells / (grid[0] * grid[1]))
+            extra["init"]["host_cores"] = po.num_threads()
+            extra["init"]["host_sample"] = ("the same generator on the host (oracle library copy, all cores) for the "
+                                            "CPU sample's slab, scaled by planes")
         tcur = po.run(om, cst, 0.0, 1)
         c0 = time.perf_counter()
         nst = 2
@@ -587,6 +627,7 @@ def _result(args, wl, grid, N, P, nsol, world, rank, ms, value, kt, launches, fr
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
+        **(extra or {}),
     }
 
 
