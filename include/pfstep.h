@@ -112,6 +112,12 @@ typedef struct {
     double nple1_a[9], nple1_b[9], nple1_c[9]; /* parsed, unused by the step */
     double nple2_a[9], nple2_b[9], nple2_c[9]; /* parsed, unused by the step */
     double eq_a[9], eq_b[9], eq_c[9];          /* PARA equilibrium wt% = a*T^2 + b*T + c */
+    /* 0: the thermo file's linear entropy and quadratic PARA lines
+     * (thermo_data.cpp:24-41, driving force solver.cpp:374-387).
+     * 1: the Fortran model's piecewise polynomial para lines and its linear
+     * driving force (Fortran_openmp_phase_field/PFM/src/sparse.f90:500-528,
+     * 797-923), selected by a thermo file whose first word is F90_POLYNOMIAL. */
+    int thermo_model;
 } pf_model;
 
 /* Per-step parameters evaluated on the host (Update_parameter,
@@ -131,6 +137,10 @@ typedef struct {
     double entropy[9], eq[9], dcdT[9];
     double D[2][3];
     double k[2][9], c[2][9];
+    /* Driving force form: 0 = entropy*(c_i - eq_ij)/dcdT_ij; 1 (thermo_model 1)
+     * = -df_ratio_ij * (max(c_i, c_j) - df_ref) */
+    int df_model;
+    double df_ratio[9], df_ref;
 } pf_step_params;
 
 /* Seeded synthetic microstructure (replaces the reference's unseeded

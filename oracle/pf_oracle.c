@@ -73,6 +73,66 @@ static double model_dims(const pfo_model *m) {
 
 /* phase_field.cpp:307-315 (Update_parameter, without the time increment),
  * thermo_data.cpp:24-41 (Get_data), phase_field.cpp:247-248 (sub-cycling). */
+/* The Fortran intercritical-annealing model's thermodynamics
+ * (Fortran_openmp_phase_field/PFM/src/sparse.f90:797-923 THERMO_DATA, with
+ * poly4 / diff_poly4 of util_func.f90:491-503): para equilibrium lines
+ * Ref_c_para and slopes 1/diff_poly4; Ref_c_para(1,3) = (1,2), (3,1) = (2,3)
+ * = (3,2) = (2,1) (sparse.f90:882-889); the diagonal keeps the initial
+ * Ref_c_para = 0, Slope_para = 1 (pre_process.f90:139-140).  In the C++
+ * model's terms eq_ij = Ref_c_para(i,j) and dcdT_ij = diff_poly4, so the
+ * partition of thermo_data.cpp:34-40 that follows is Partition_k_para(j,i),
+ * Partition_c_para(j,i).  Ratio_k_para (sparse.f90:916-921) drives the
+ * austenite pairs: driving_force = -Ratio_k_para(i,j) (max(c_i, c_j) -
+ * Ref_c_para(2,1)) (sparse.f90:512-515; the stored energy of deformed grains
+ * is not modelled).  Double precision (the Fortran declares default REAL). */
+static double f90_poly4(double x, double a, double b, double c, double d) {
+    return a * x + b * x * x + c * x * x * x + d * x * x * x * x;
+}
+static double f90_diff_poly4(double x, double a, double b, double c, double d) {
+    return a + 2 * b * x + 3 * c * x * x + 4 * d * x * x * x;
+}
+static void f90_thermo(double T, pfo_params *p) {
+    double ref[9], slope_d[9], ratio[9];
+    for (int e = 0; e < 9; e++) {
+        ref[e] = 0.;
+        slope_d[e] = 1.;
+        ratio[e] = 0.;
+    }
+    if (T < 1086.52) {
+        M3(ref, 1, 2) = f90_poly4(T - 273.15, -8.309e-5, 0., 0., 0.) + 6.883e-2;
+        M3(ref, 2, 1) = f90_poly4(T - 273.15, 2.607e-2, -6.58e-5, 3.984e-8, 0.) + 0.9115;
+        M3(slope_d, 1, 2) = f90_diff_poly4(T - 273.15, -8.309e-5, 0., 0., 0.);
+        M3(slope_d, 2, 1) = f90_diff_poly4(T - 273.15, 2.607e-2, -6.58e-5, 3.984e-8, 0.);
+    } else {
+        M3(ref, 1, 2) = f90_poly4(T - 1086.52, -1.1428e-4, 0., 0., 0.);
+        M3(ref, 2, 1) = f90_poly4(T - 1086.52, -0.00325, 0., 0., 0.);
+        M3(slope_d, 1, 2) = f90_diff_poly4(0., -1.1428e-4, -1.78883e-7, -3.66186e-10, 2.53049e-12);
+        M3(slope_d, 2, 1) = f90_diff_poly4(0., -0.00325, 1.13712e-5, -2.88193e-8, 1.05482e-10);
+    }
+    M3(ref, 1, 3) = M3(ref, 1, 2);
+    M3(ref, 3, 1) = M3(ref, 2, 1);
+    M3(slope_d, 1, 3) = M3(slope_d, 1, 2);
+    M3(slope_d, 3, 1) = M3(slope_d, 2, 1);
+    M3(ref, 2, 3) = M3(ref, 2, 1);
+    M3(ref, 3, 2) = M3(ref, 2, 1);
+    M3(slope_d, 2, 3) = M3(slope_d, 2, 1);
+    M3(slope_d, 3, 2) = M3(slope_d, 2, 1);
+    const double x = T - 273.15;
+    M3(ratio, 1, 2) = (0.000264 * x * x - 0.4466 * x + 243.4713) * 1.03e-12;
+    M3(ratio, 2, 1) = -M3(ratio, 1, 2);
+    M3(ratio, 3, 2) = M3(ratio, 1, 2);
+    M3(ratio, 2, 3) = -M3(ratio, 3, 2);
+    M3(ratio, 2, 2) = 0.;
+    for (int e = 0; e < 9; e++) {
+        p->entropy[e] = 0.;
+        p->eq[e] = ref[e];
+        p->dcdT[e] = slope_d[e];
+        p->df_ratio[e] = ratio[e];
+    }
+    p->df_ref = M3(ref, 2, 1);
+    p->df_model = 1;
+}
+
 void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
     memset(p, 0, sizeof(*p));
     const double T = pfo_temperature(m, time);
@@ -95,15 +155,20 @@ void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
     p->pfm_dt = m->dx * m->dx / p->dims * 0.2 / maxms;
     p->diff_dt = m->dx * m->dx / maxD / p->dims * 0.2;
 
-    /* thermo_data.cpp:25-32: functor evaluation; linear_functor.h:11-13,
-     * quadratic_functor.h:12-14.  Unset functors are zero. */
-    for (int j = 1; j <= 3; j++)
-        for (int i = 1; i <= 3; i++) {
-            const double x = T;
-            M3(p->entropy, i, j) = M3(m->ent_a, i, j) * x + M3(m->ent_b, i, j);
-            M3(p->eq, i, j) = M3(m->eq_a, i, j) * x * x + M3(m->eq_b, i, j) * x + M3(m->eq_c, i, j);
-            M3(p->dcdT, i, j) = (2 * M3(m->eq_a, i, j)) * x + M3(m->eq_b, i, j);
-        }
+    p->df_model = 0;
+    if (m->thermo_model == 1) {
+        f90_thermo(T, p);
+    } else {
+        /* thermo_data.cpp:25-32: functor evaluation; linear_functor.h:11-13,
+         * quadratic_functor.h:12-14.  Unset functors are zero. */
+        for (int j = 1; j <= 3; j++)
+            for (int i = 1; i <= 3; i++) {
+                const double x = T;
+                M3(p->entropy, i, j) = M3(m->ent_a, i, j) * x + M3(m->ent_b, i, j);
+                M3(p->eq, i, j) = M3(m->eq_a, i, j) * x * x + M3(m->eq_b, i, j) * x + M3(m->eq_c, i, j);
+                M3(p->dcdT, i, j) = (2 * M3(m->eq_a, i, j)) * x + M3(m->eq_b, i, j);
+            }
+    }
     /* thermo_data.cpp:34-40 */
     for (int i = 1; i <= 3; i++)
         for (int j = 1; j <= 3; j++) {
@@ -148,11 +213,17 @@ void pfo_partition_all(const pfo_model *m, const pfo_params *p, const double *ph
     }
 }
 
-/* solver.cpp:374-387 (Driving_force); uses only the carbon concentration of phase ii */
-static inline double driving_force(const pfo_params *p, int phii, int phjj, double concii) {
+/* solver.cpp:374-387 (Driving_force); uses only the carbon concentration of
+ * phase ii -- or, with the Fortran model's thermodynamics, the larger of the
+ * two phases' carbon (sparse.f90:512-515). */
+static inline double driving_force(const pfo_params *p, int phii, int phjj, double concii, double concjj) {
     double df = 0.;
-    if (phii != phjj)
-        df += M3(p->entropy, phii, phjj) * (concii - M3(p->eq, phii, phjj)) / M3(p->dcdT, phii, phjj);
+    if (phii != phjj) {
+        if (p->df_model == 1)
+            df -= M3(p->df_ratio, phii, phjj) * (fmax(concii, concjj) - p->df_ref);
+        else
+            df += M3(p->entropy, phii, phjj) * (concii - M3(p->eq, phii, phjj)) / M3(p->dcdT, phii, phjj);
+    }
     return df;
 }
 
@@ -236,7 +307,7 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
             d += (sv1[ii] - sv1[jj]) * factor2;
             d *= M3(m->sigma, phi_, phj);
             d += factor3 * sqrt(sv1[ii] * sv1[jj]) *
-                 driving_force(p, phi_, phj, local_conc[phi_]);
+                 driving_force(p, phi_, phj, local_conc[phi_], local_conc[phj]);
             d *= M3(p->m, phi_, phj);
             del[ii] += d;
         }

@@ -50,6 +50,7 @@ typedef struct {
     double ent_a[9], ent_b[9];    /* entropy functor a*T+b  (thermo_functor.cpp:20-25) */
     double eq_a[9], eq_b[9], eq_c[9]; /* PARA functor a*T^2+b*T+c (thermo_functor.cpp:45-50) */
     double mn_ratio[3];           /* Mn partition ratios r_p: c_p = r_p * c_ref (solute 2 only) */
+    int thermo_model;             /* 1: the Fortran model's polynomial thermodynamics (sparse.f90:797-923) */
 } pfo_model;
 
 typedef struct {
@@ -63,6 +64,8 @@ typedef struct {
     double k[PFO_MAXSOL][9], c[PFO_MAXSOL][9];
     double dims;                  /* 'dimensions' is a real in the reference */
     double eta;
+    int df_model;                 /* 1: driving force -ratio_ij*(max(c_i,c_j) - ref) (sparse.f90:512-515) */
+    double df_ratio[9], df_ref;
 } pfo_params;
 
 typedef struct {

@@ -38,6 +38,7 @@ class OModel(ctypes.Structure):
         ("ent_a", _d9), ("ent_b", _d9),
         ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
         ("mn_ratio", _d3),
+        ("thermo_model", ctypes.c_int),
     ]
 
 
@@ -52,6 +53,8 @@ class OParams(ctypes.Structure):
         ("entropy", _d9), ("eq", _d9), ("dcdT", _d9),
         ("k", _d9 * 2), ("c", _d9 * 2),
         ("dims", ctypes.c_double), ("eta", ctypes.c_double),
+        ("df_model", ctypes.c_int),
+        ("df_ratio", _d9), ("df_ref", ctypes.c_double),
     ]
 
 
@@ -148,9 +151,14 @@ def _e(i: int, j: int) -> int:
 
 
 def parse_thermo(path: str, out: dict) -> None:
-    s = _Stream(open(path).read())
+    text = open(path).read()
     for k in ("ent_a", "ent_b", "eq_a", "eq_b", "eq_c"):
         out[k] = [0.0] * 9
+    out["thermo_model"] = 0
+    if text.split()[:1] == ["F90_POLYNOMIAL"]:  # the Fortran model's built-in polynomials
+        out["thermo_model"] = 1
+        return
+    s = _Stream(text)
     s.ignore(3)
     for _ in range(3):
         i, j = s.read(int), s.read(int)
@@ -240,6 +248,7 @@ def model_from_dict(d: dict) -> OModel:
         for e, v in enumerate(d[k]):
             arr[e] = v
     m.nsol = d["nsol"]
+    m.thermo_model = d.get("thermo_model", 0)
     for q in range(2):
         for p in range(3):
             m.D0[q][p], m.DQ[q][p] = d["D0"][q][p], d["DQ"][q][p]

@@ -66,6 +66,7 @@ class PfModel(ctypes.Structure):
         ("nple1_a", _d9), ("nple1_b", _d9), ("nple1_c", _d9),
         ("nple2_a", _d9), ("nple2_b", _d9), ("nple2_c", _d9),
         ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
+        ("thermo_model", ctypes.c_int),
     ]
 
 
@@ -85,6 +86,8 @@ class PfStepParams(ctypes.Structure):
         ("entropy", _d9), ("eq", _d9), ("dcdT", _d9),
         ("D", _d3 * 2),
         ("k", _d9 * 2), ("c", _d9 * 2),
+        ("df_model", ctypes.c_int),
+        ("df_ratio", _d9), ("df_ref", ctypes.c_double),
     ]
 
 

@@ -868,6 +868,8 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
 extern "C" int pf_adj_create(const pf_model *model, int precision, int checkpoint_every, pf_adj **out) {
     if (!model || !out || checkpoint_every < 1) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad arguments");
     if (precision != PF_PREC_FP64 && precision != PF_PREC_FP32C) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad precision");
+    if (model->thermo_model != 0)
+        return pf_fail(PF_ERR_ARG, "pf_adj_create: the adjoint differentiates the linear-line thermodynamics only");
     *out = nullptr;
     pf_adj *a = new pf_adj();
     a->prec = precision;

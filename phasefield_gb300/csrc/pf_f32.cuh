@@ -160,6 +160,8 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     //   X = S_i phi_j - S_j phi_i and Y = phi_i - phi_j flip sign between (i,j)
     //   and (j,i), Z = sqrt(phi_i phi_j) does not; A, B are symmetric in the
     //   phase pair, G and E are not.  A = B = G = 0 for pairs that do not interact.
+    //   The driving term is G (c_i - E), or G (max(c_i, c_j) - E) with the
+    //   Fortran model's thermodynamics (P.dfmax).
     for (int a = 0; a < num; a++) L.del[a][t] = 0.f;
     for (int a = 0; a < num; a++) {
         const int ia = L.id[a][t];
@@ -176,8 +178,9 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
             const float Z = sqrtf(va1 * vb1);
             const float sym = P.A[e] * X + P.B[e] * Y;
             const float cb = pb == 1 ? lc[0] : (pb == 2 ? lc[1] : lc[2]);
-            da += sym + P.G[e] * Z * (ca - P.E[e]);
-            L.del[b][t] += -sym + P.G[ee] * Z * (cb - P.E[ee]);
+            const float xa = P.dfmax ? fmaxf(ca, cb) : ca, xb = P.dfmax ? fmaxf(ca, cb) : cb;
+            da += sym + P.G[e] * Z * (xa - P.E[e]);
+            L.del[b][t] += -sym + P.G[ee] * Z * (xb - P.E[ee]);
         }
         float d = va1 + da;
         if (d > 1.0f) d = 1.0f;
@@ -361,8 +364,9 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
                     const float Y = v1[a] - v1[b];
                     const float Z = sqrtf(v1[a] * v1[b]);
                     const float sym = P.A[e] * X + P.B[e] * Y;
-                    da += sym + P.G[e] * Z * (ce[a] - P.E[e]);
-                    del[b] += -sym + P.G[ee] * Z * (ce[b] - P.E[ee]);
+                    const float xa = P.dfmax ? fmaxf(ce[a], ce[b]) : ce[a], xb = P.dfmax ? fmaxf(ce[a], ce[b]) : ce[b];
+                    da += sym + P.G[e] * Z * (xa - P.E[e]);
+                    del[b] += -sym + P.G[ee] * Z * (xb - P.E[ee]);
                 }
             }
             float d = v1[a] + da;

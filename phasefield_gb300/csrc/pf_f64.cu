@@ -16,12 +16,15 @@
 namespace {
 
 // Driving_force (solver.cpp:374-387) for a phase pair, given the cell's carbon
-// concentration of phase pi.  df = 0.; df += ... is kept literally.
-__device__ __forceinline__ double pf_df(const pf_step_params &P, int pi, int pj, double conc_pi) {
+// concentrations of phases pi and pj.  df = 0.; df += ... is kept literally.
+// With the Fortran model's thermodynamics (df_model 1) it is
+// -Ratio_k_para(pi,pj) * (max(c_pi, c_pj) - Ref_c_para(2,1)) (sparse.f90:512-515).
+__device__ __forceinline__ double pf_df(const pf_step_params &P, int pi, int pj, double conc_pi, double conc_pj) {
     double df = 0.;
     if (pi != pj) {
         const int e = (pi - 1) + 3 * (pj - 1);
-        df += P.entropy[e] * (conc_pi - P.eq[e]) / P.dcdT[e];
+        if (P.df_model == 1) df -= P.df_ratio[e] * (fmax(conc_pi, conc_pj) - P.df_ref);
+        else df += P.entropy[e] * (conc_pi - P.eq[e]) / P.dcdT[e];
     }
     return df;
 }
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
 #pragma unroll
     for (int a = 1; a <= 3; a++)
 #pragma unroll
-        for (int b = 1; b <= 3; b++) df[(a - 1) + 3 * (b - 1)] = pf_df(P, a, b, lc[a - 1]);
+        for (int b = 1; b <= 3; b++) df[(a - 1) + 3 * (b - 1)] = pf_df(P, a, b, lc[a - 1], lc[b - 1]);
 
     const double factor1 = P.factor1, factor2 = P.factor2, factor3 = P.factor3;
     double del[PF_NSTENCIL];

@@ -72,6 +72,17 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
         m->nple2_a[e] = m->nple2_b[e] = m->nple2_c[e] = 0.;
         m->eq_a[e] = m->eq_b[e] = m->eq_c[e] = 0.;
     }
+    m->thermo_model = 0;
+    {
+        std::string word;
+        f >> word;
+        if (word == "F90_POLYNOMIAL") {  // every coefficient is built in (pf_f90_thermo)
+            m->thermo_model = 1;
+            return PF_OK;
+        }
+        f.clear();
+        f.seekg(0);
+    }
     for (int t = 0; t < 3; t++) f.ignore(1000, '\n');
     int i, j;
     double a, b, c;
@@ -249,6 +260,58 @@ static double pf_temperature(const pf_model &m, double t) {
     return Temp;
 }
 
+// The Fortran model's thermodynamics at temperature T (sparse.f90:797-923,
+// Poly4/Diff_poly4 of util_func.f90:491-503), in the C++ model's terms: eq_ij
+// = Ref_c_para(i,j), dcdT_ij = 1/Slope_para(i,j) (diagonal: eq 0, dcdT 1, the
+// initial values of pre_process.f90:139-140), so the partition k_ij, c_ij that
+// follows (thermo_data.cpp:34-40) equals the Fortran Partition_k_para(j,i),
+// Partition_c_para(j,i); the driving force of an austenite pair is
+// -Ratio_k_para(i,j) * (max(c_i, c_j) - Ref_c_para(2,1)) (sparse.f90:500-528,
+// without the stored energy of deformed grains).  Evaluated in double (the
+// Fortran source declares default REAL).
+void pf_f90_thermo(double T, pf_step_params &p) {
+    auto poly4 = [](double x, double a, double b, double c, double d) {
+        return a * x + b * x * x + c * x * x * x + d * x * x * x * x;
+    };
+    auto dpoly4 = [](double x, double a, double b, double c, double d) {
+        return a + 2 * b * x + 3 * c * x * x + 4 * d * x * x * x;
+    };
+    double ref12, ref21, dcdt12, dcdt21;
+    if (T < 1086.52) {
+        const double x = T - 273.15;
+        ref12 = poly4(x, -8.309e-5, 0., 0., 0.) + 6.883e-2;
+        ref21 = poly4(x, 2.607e-2, -6.58e-5, 3.984e-8, 0.) + 0.9115;
+        dcdt12 = dpoly4(x, -8.309e-5, 0., 0., 0.);
+        dcdt21 = dpoly4(x, 2.607e-2, -6.58e-5, 3.984e-8, 0.);
+    } else {
+        const double x = T - 1086.52;
+        ref12 = poly4(x, -1.1428e-4, 0., 0., 0.);
+        ref21 = poly4(x, -0.00325, 0., 0., 0.);
+        dcdt12 = dpoly4(0., -1.1428e-4, -1.78883e-7, -3.66186e-10, 2.53049e-12);
+        dcdt21 = dpoly4(0., -0.00325, 1.13712e-5, -2.88193e-8, 1.05482e-10);
+    }
+    for (int e = 0; e < 9; e++) {
+        p.eq[e] = 0.;
+        p.dcdT[e] = 1.;
+        p.entropy[e] = 0.;
+        p.df_ratio[e] = 0.;
+    }
+    // (1,2) and (1,3) take the ferrite line; (2,1), (3,1), (2,3), (3,2) the
+    // austenite line (sparse.f90:882-889).
+    p.eq[e3(1, 2)] = p.eq[e3(1, 3)] = ref12;
+    p.dcdT[e3(1, 2)] = p.dcdT[e3(1, 3)] = dcdt12;
+    p.eq[e3(2, 1)] = p.eq[e3(3, 1)] = p.eq[e3(2, 3)] = p.eq[e3(3, 2)] = ref21;
+    p.dcdT[e3(2, 1)] = p.dcdT[e3(3, 1)] = p.dcdT[e3(2, 3)] = p.dcdT[e3(3, 2)] = dcdt21;
+    const double x = T - 273.15;
+    const double r12 = (0.000264 * x * x - 0.4466 * x + 243.4713) * 1.03e-12;  // sparse.f90:916-921
+    p.df_ratio[e3(1, 2)] = r12;
+    p.df_ratio[e3(2, 1)] = -r12;
+    p.df_ratio[e3(3, 2)] = r12;
+    p.df_ratio[e3(2, 3)] = -r12;
+    p.df_ref = ref21;
+    p.df_model = 1;
+}
+
 void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
     std::memset(&p, 0, sizeof(p));
     p.ix = m.ix; p.iy = m.iy; p.iz = m.iz;
@@ -280,14 +343,18 @@ void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
         }
     p.pfm_dt = m.dx * m.dx / dims * 0.2 / maxms;
     p.diff_dt = m.dx * m.dx / maxD / dims * 0.2;
-    // thermo_data.cpp:25-32 with linear_functor.h / quadratic_functor.h
-    for (int j = 1; j <= 3; j++)
-        for (int i = 1; i <= 3; i++) {
-            const int e = e3(i, j);
-            p.entropy[e] = m.ent_a[e] * T + m.ent_b[e];
-            p.eq[e] = m.eq_a[e] * T * T + m.eq_b[e] * T + m.eq_c[e];
-            p.dcdT[e] = (2 * m.eq_a[e]) * T + m.eq_b[e];
-        }
+    if (m.thermo_model == 1) {
+        pf_f90_thermo(T, p);
+    } else {
+        // thermo_data.cpp:25-32 with linear_functor.h / quadratic_functor.h
+        for (int j = 1; j <= 3; j++)
+            for (int i = 1; i <= 3; i++) {
+                const int e = e3(i, j);
+                p.entropy[e] = m.ent_a[e] * T + m.ent_b[e];
+                p.eq[e] = m.eq_a[e] * T * T + m.eq_b[e] * T + m.eq_c[e];
+                p.dcdT[e] = (2 * m.eq_a[e]) * T + m.eq_b[e];
+            }
+    }
     // thermo_data.cpp:34-40
     for (int i = 1; i <= 3; i++)
         for (int j = 1; j <= 3; j++) {
@@ -327,6 +394,7 @@ void pf_fold_f32(const pf_step_params &p, int b1, int b2, pf_f32_params &f) {
     f.N = p.N;
     f.b1 = b1; f.b2 = b2;
     f.cutoff = (float)p.cutoff;
+    f.dfmax = p.df_model == 1 ? 1 : 0;
     for (int i = 1; i <= 3; i++)
         for (int j = 1; j <= 3; j++) {
             const int e = e3(i, j);
@@ -334,8 +402,13 @@ void pf_fold_f32(const pf_step_params &p, int b1, int b2, pf_f32_params &f) {
             const double dm = p.pfm_dt * p.m[e];
             f.A[e] = inter ? (float)(dm * p.sigma[e] * p.factor1) : 0.f;
             f.B[e] = inter ? (float)(dm * p.sigma[e] * p.factor2) : 0.f;
-            f.G[e] = (inter && i != j) ? (float)(dm * p.factor3 * p.entropy[e] / p.dcdT[e]) : 0.f;
-            f.E[e] = (float)p.eq[e];
+            if (p.df_model == 1) {  // G * (max(c_i, c_j) - E)
+                f.G[e] = (inter && i != j) ? (float)(-dm * p.factor3 * p.df_ratio[e]) : 0.f;
+                f.E[e] = (float)p.df_ref;
+            } else {                // G * (c_i - E)
+                f.G[e] = (inter && i != j) ? (float)(dm * p.factor3 * p.entropy[e] / p.dcdT[e]) : 0.f;
+                f.E[e] = (float)p.eq[e];
+            }
         }
     for (int q = 0; q < p.nsol; q++) {
         for (int ph = 0; ph < 3; ph++) f.D[q][ph] = (float)(p.D[q][ph] * p.coef_diff);

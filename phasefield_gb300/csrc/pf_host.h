@@ -8,6 +8,9 @@ int pf_fail(int status, const std::string &msg);
 // Per-step parameters (phase_field.cpp:307-315, thermo_data.cpp:24-41,
 // phase_field.cpp:247-248); 'time' is the time at the start of the step.
 void pf_compute_params(const pf_model &m, double time, pf_step_params &p);
+// The Fortran model's thermodynamics (thermo_model 1) at temperature T:
+// eq, dcdT, entropy, df_model, df_ratio, df_ref of p.
+void pf_f90_thermo(double T, pf_step_params &p);
 // Fold FP64 step parameters into the FP32 kernels' block.
 struct pf_f32_map;
 void pf_fold_f32(const pf_step_params &p, int b1, int b2, pf_f32_params &f);

@@ -30,6 +30,7 @@ typedef struct {
     long long N;
     int b1, b2;                 // local grain id -> phase: id<=b1 ->1, <=b2 ->2, else 3
     float cutoff;
+    int dfmax;                  // 1: pair driving term G*(max(c_i, c_j) - E) (Fortran thermodynamics)
     float A[9];                 // dt*m*sigma*f1
     float B[9];                 // dt*m*sigma*f2
     float G[9];                 // dt*m*f3*entropy/dcdT

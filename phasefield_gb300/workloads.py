@@ -67,9 +67,17 @@ _PAIRS = ["ferrite-ferrite", "ferrite-austenite", "ferrite-cementite",
 _PHASES = ["ferrite", "austenite", "cementite"]
 
 
-def write_thermo(path: str) -> str:
+# Selects the Fortran intercritical-annealing model's thermodynamics
+# (Fortran_openmp_phase_field/PFM/src/sparse.f90:797-923): piecewise polynomial
+# para lines and the linear austenite driving force, all coefficients built in.
+THERMO_F90_TEXT = """F90_POLYNOMIAL
+# para/NPLE lines of the Fortran model (sparse.f90:797-923); no coefficients here
+"""
+
+
+def write_thermo(path: str, model: str = "linear") -> str:
     with open(path, "w") as f:
-        f.write(THERMO_TEXT)
+        f.write(THERMO_F90_TEXT if model == "f90" else THERMO_TEXT)
     return path
 
 

@@ -1,0 +1,104 @@
+"""The Fortran model's thermodynamics as a selectable model (thermo file
+F90_POLYNOMIAL): piecewise polynomial para lines, their slopes and the linear
+austenite driving force of Fortran_openmp_phase_field/PFM/src/sparse.f90:
+500-528 and 797-923.  The product's parameters equal the oracle's bit for bit,
+and both agree with a literal restatement of the Fortran route (slopes
+1/diff_poly4, Partition_k = transpose(Slope)/Slope, Partition_c = Ref -
+Partition_k * transpose(Ref)) written out here."""
+import os
+
+import numpy as np
+import pytest
+
+import phasefield_gb300 as pf
+import pyoracle as po
+from phasefield_gb300 import workloads as W
+
+
+def _case(tmp, grid=(64, 48, 1), T=1023.0):
+    W.write_thermo(os.path.join(tmp, "thermo_f90.txt"), "f90")
+    cfg = W.write_config(os.path.join(tmp, "f90.txt"), grid=grid, T=T, thermo_file="thermo_f90.txt",
+                         directory=os.path.join(tmp, "out"))
+    return cfg, pf.read_model(cfg), po.load_model(cfg)
+
+
+def _fortran_route(T):
+    """sparse.f90:797-923 literally (Ref_c_para, Slope_para, Partition_k_para,
+    Partition_c_para, Ratio_k_para), 0-based 3x3 arrays [i][j]."""
+    poly4 = lambda x, a, b, c, d: a * x + b * x * x + c * x * x * x + d * x * x * x * x
+    dpoly4 = lambda x, a, b, c, d: a + 2 * b * x + 3 * c * x * x + 4 * d * x * x * x
+    ref = np.zeros((3, 3))
+    slope = np.ones((3, 3))
+    if T < 1086.52:
+        ref[0, 1] = poly4(T - 273.15, -8.309e-5, 0, 0, 0) + 6.883e-2
+        ref[1, 0] = poly4(T - 273.15, 2.607e-2, -6.58e-5, 3.984e-8, 0) + 0.9115
+        slope[0, 1] = 1.0 / dpoly4(T - 273.15, -8.309e-5, 0, 0, 0)
+        slope[1, 0] = 1.0 / dpoly4(T - 273.15, 2.607e-2, -6.58e-5, 3.984e-8, 0)
+    else:
+        ref[0, 1] = poly4(T - 1086.52, -1.1428e-4, 0, 0, 0)
+        ref[1, 0] = poly4(T - 1086.52, -0.00325, 0, 0, 0)
+        slope[0, 1] = 1.0 / dpoly4(0, -1.1428e-4, -1.78883e-7, -3.66186e-10, 2.53049e-12)
+        slope[1, 0] = 1.0 / dpoly4(0, -0.00325, 1.13712e-5, -2.88193e-8, 1.05482e-10)
+    ref[0, 2], ref[2, 0] = ref[0, 1], ref[1, 0]
+    slope[0, 2], slope[2, 0] = slope[0, 1], slope[1, 0]
+    ref[1, 2] = ref[2, 1] = ref[1, 0]
+    slope[1, 2] = slope[2, 1] = slope[1, 0]
+    pk = slope.T / slope
+    pc = ref - pk * ref.T
+    x = T - 273.15
+    ratio = np.zeros((3, 3))
+    ratio[0, 1] = (0.000264 * x * x - 0.4466 * x + 243.4713) * 1.03e-12
+    ratio[1, 0] = -ratio[0, 1]
+    ratio[2, 1] = ratio[0, 1]
+    ratio[1, 2] = -ratio[2, 1]
+    return ref, pk, pc, ratio
+
+
+def _m3(arr):
+    """Column-major 3x3 (i,j) at (i-1)+3(j-1) -> [i][j]."""
+    return np.array([[arr[i + 3 * j] for j in range(3)] for i in range(3)])
+
+
+@pytest.mark.parametrize("T", [900.0, 1013.0, 1023.0, 1086.0, 1090.0, 1150.0])
+def test_f90_parameters_product_oracle_and_fortran_route(tmp_path, T):
+    cfg, m, om = _case(str(tmp_path), T=T)
+    assert m.thermo_model == 1 and om.thermo_model == 1
+    p, q = pf.params_at(m, 0.0), po.params_at(om, 0.0)
+    assert p.T == T and q.T == T
+    assert p.df_model == 1 and q.df_model == 1 and p.df_ref == q.df_ref
+    for name in ("eq", "dcdT", "df_ratio"):
+        assert list(getattr(p, name)) == list(getattr(q, name)), name
+    assert list(p.k[0]) == list(q.k[0]) and list(p.c[0]) == list(q.c[0])
+    ref, pk, pc, ratio = _fortran_route(T)
+    # the C++ model's k_ij, c_ij are the Fortran Partition_k(j,i), Partition_c(j,i)
+    np.testing.assert_allclose(_m3(p.k[0]), pk.T, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(_m3(p.c[0]), pc.T, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(_m3(p.df_ratio), ratio, rtol=1e-15, atol=0)
+    assert p.df_ref == pytest.approx(ref[1, 0], rel=1e-15)
+    np.testing.assert_allclose(_m3(p.eq), ref, rtol=1e-15, atol=0)
+
+
+def test_f90_model_steps_differ_from_linear_model(tmp_path):
+    """The oracle advances the same state differently under the two models
+    (the Fortran driving force is in effect), and conserves carbon."""
+    grid = (48, 40, 1)
+    cfg, m, om = _case(str(tmp_path), grid=grid)
+    W.write_thermo(str(tmp_path / "thermo_steel.txt"))
+    cfg_lin = W.write_config(str(tmp_path / "lin.txt"), grid=grid, T=1023.0, directory=str(tmp_path / "out"))
+    om_lin = po.load_model(cfg_lin)
+    spec = W.WORKLOADS["2d256"].spec()
+    spec.n_grains, spec.n_nuclei = 5, 4
+    st = po.init_state(om, spec, 0.0)
+    st_lin = {k: v.copy() for k, v in st.items()}
+    tot0 = st["C"][: 48 * 40].sum()
+    po.run(om, st, 0.0, 20)
+    po.run(om_lin, st_lin, 0.0, 20)
+    assert not np.array_equal(st["phi"], st_lin["phi"])
+    assert np.all(np.isfinite(st["phi"]))
+    assert abs(st["C"][: 48 * 40].sum() - tot0) / tot0 < 1e-12
+
+
+def test_adjoint_rejects_f90_thermodynamics(tmp_path):
+    cfg, m, om = _case(str(tmp_path))
+    h = pf.ctypes.c_void_p()
+    assert pf.lib().pf_adj_create(pf.ctypes.byref(m), pf.PF_PREC_FP64, 10, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
