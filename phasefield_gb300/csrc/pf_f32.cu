@@ -68,10 +68,12 @@ __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__
     pf_defer(defer, n, rest, rest_count);
 }
 
-// The deferred cells of k_phase_f32, one per thread, with the general
-// ten-entry list (solver.cpp:147-304 without the four-entry limit).
+// The deferred cells of k_phase_f32, one per thread: lists of up to eight
+// grains in registers, longer ones (or own slots that are not a prefix) with
+// the general ten-entry list (solver.cpp:147-304) in the thread's local
+// memory -- no shared memory, so occupancy is set by registers alone.
 template <int NSOL>
-__global__ void __launch_bounds__(kPT) k_phase_f32_rest(const __grid_constant__ pf_f32_params P,
+__global__ void __launch_bounds__(kPT, 3) k_phase_f32_rest(const __grid_constant__ pf_f32_params P,
                                                         const ushort4 *__restrict__ gid1,
                                                         const float4 *__restrict__ phi1,
                                                         ushort4 *__restrict__ gid2, float4 *__restrict__ phi2,
@@ -79,14 +81,24 @@ __global__ void __launch_bounds__(kPT) k_phase_f32_rest(const __grid_constant__ 
                                                         const float2 *__restrict__ sol,
                                                         const unsigned int *__restrict__ rest,
                                                         const unsigned int *__restrict__ rest_count) {
-    __shared__ pf_plist<kPT> L;
     const unsigned cnt = *rest_count;
-    const unsigned ix = (unsigned)P.ix, iy = (unsigned)P.iy;
+    const unsigned ix = (unsigned)P.ix, iy = (unsigned)P.iy, iz = (unsigned)P.iz;
+    const unsigned plane = ix * iy;
     for (unsigned q = blockIdx.x * kPT + threadIdx.x; q < cnt; q += gridDim.x * kPT) {
         const unsigned n = rest[q];
         const unsigned r = n / ix;
-        pf_phase_cell<NSOL, kPT>(P, (int)(n - r * ix), (int)(r % iy), (int)(r / iy), threadIdx.x, gid1, phi1,
-                                 gid2, phi2, sphase, sol, L);
+        const int i = (int)(n - r * ix), j = (int)(r % iy), k = (int)(r / iy);
+        unsigned nb[6];
+        nb[0] = n - i + pf_wrap(i, (int)ix, -1);
+        nb[1] = n - i + pf_wrap(i, (int)ix, 1);
+        nb[2] = n + ix * (pf_wrap(j, (int)iy, -1) - j);
+        nb[3] = n + ix * (pf_wrap(j, (int)iy, 1) - j);
+        nb[4] = n + plane * (pf_wrap(k, (int)iz, -1) - k);
+        nb[5] = n + plane * (pf_wrap(k, (int)iz, 1) - k);
+        if (!pf_phase_cell_reg<NSOL, false, 8>(P, n, nb, gid1, phi1, gid2, phi2, sphase, sol)) {
+            pf_plist<1> L;
+            pf_phase_cell<NSOL, 1>(P, i, j, k, 0, gid1, phi1, gid2, phi2, sphase, sol, L);
+        }
     }
 }
 
@@ -298,8 +310,8 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
                                 unsigned int *rest, unsigned int *rest_count, cudaStream_t s) {
     const dim3 block(kPX, kPY);
     const dim3 grid((unsigned)((P.ix + kPX - 1) / kPX), (unsigned)((P.iy + kPY - 1) / kPY), (unsigned)P.iz);
-    long long rb = (P.N / 64 + kPT - 1) / kPT;  // the rest kernel loops if more than 1/64 of the cells wait
-    if (rb > 152 * 5) rb = 152 * 5;
+    long long rb = (P.N / 32 + kPT - 1) / kPT;  // the rest kernel loops if more than 1/32 of the cells wait
+    if (rb > 152 * 8) rb = 152 * 8;
     if (rb < 1) rb = 1;
     cudaError_t e = cudaMemsetAsync(rest_count, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;

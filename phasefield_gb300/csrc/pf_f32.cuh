@@ -230,19 +230,19 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
     sphase[2 * N + n] = sqrtf(ph[2] * inv);
 }
 
-// The same update for a cell whose merged stencil list has at most four
-// grains -- about 98% of the cells of 3D Voronoi/nucleus microstructures --
-// with the list held in registers: the merge compares each neighbour slot
-// with the four entries at once, the pair loop, the clamps and the top-four
-// selection are unrolled over the four entries with the list length as a
-// predicate, so the lanes of a warp stay together.  The entry order, the
+// The same update for a cell whose merged stencil list has at most K grains
+// (K = 4 covers about 98% of the cells of 3D Voronoi/nucleus
+// microstructures) with the list held in registers: the merge compares each
+// neighbour slot with the K entries at once, the pair loop, the clamps and
+// the top-four selection are unrolled over the K entries with the list
+// length as a predicate, so the lanes of a warp stay together.  The entry order, the
 // summation order of every pair term and the selection rule are those of
 // pf_phase_cell, so both routes give the same values for such a cell.
 // Returns false, having written nothing, for a cell the register list cannot
-// hold (a fifth grain in the stencil, or own slots above the cutoff that are
-// not a prefix); the caller routes that cell to pf_phase_cell.  Cell indices
+// hold (a (K+1)-th grain in the stencil, or own slots above the cutoff that
+// are not a prefix); the caller routes that cell to pf_phase_cell.  Cell indices
 // are 32-bit (grids of fewer than 2^32 cells).
-template <int NSOL, bool CG = false>
+template <int NSOL, bool CG = false, int K = 4>
 __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsigned n, const unsigned nb[6],
                                                   const ushort4 *__restrict__ gid1,
                                                   const float4 *__restrict__ phi1, ushort4 *__restrict__ gid2,
@@ -279,9 +279,17 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
     // solver.cpp:168-177: own slots above the cutoff, in slot order.
     const bool ok0 = v.x > cutoff, ok1 = v.y > cutoff, ok2 = v.z > cutoff, ok3 = v.w > cutoff;
     if ((ok1 && !ok0) || (ok2 && !ok1) || (ok3 && !ok2)) return false;
-    int lid[4] = {ok0 ? (int)g.x : 0, ok1 ? (int)g.y : 0, ok2 ? (int)g.z : 0, ok3 ? (int)g.w : 0};
-    float v1[4] = {ok0 ? v.x : 0.f, ok1 ? v.y : 0.f, ok2 ? v.z : 0.f, ok3 ? v.w : 0.f};
-    float v2[4] = {0.f, 0.f, 0.f, 0.f};
+    static_assert(K >= 4 && K <= PF_NSTENCIL, "the register list holds the own slots");
+    int lid[K];
+    float v1[K], v2[K];
+#pragma unroll
+    for (int e = 0; e < K; e++) {
+        lid[e] = 0;
+        v1[e] = 0.f;
+        v2[e] = 0.f;
+    }
+    lid[0] = ok0 ? (int)g.x : 0; lid[1] = ok1 ? (int)g.y : 0; lid[2] = ok2 ? (int)g.z : 0; lid[3] = ok3 ? (int)g.w : 0;
+    v1[0] = ok0 ? v.x : 0.f; v1[1] = ok1 ? v.y : 0.f; v1[2] = ok2 ? v.z : 0.f; v1[3] = ok3 ? v.w : 0.f;
     int num = (int)ok0 + (int)ok1 + (int)ok2 + (int)ok3;
     // solver.cpp:179-205: neighbours x-, x+, y-, y+, z-, z+, each scanned to
     // its first empty slot; an id already listed adds its value, a new id is
@@ -301,15 +309,15 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
                     const float tv = nvv[a];
                     bool hit = false;
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
+                    for (int e = 0; e < K; e++) {
                         const bool m = lid[e] == tid;
                         if (m) v2[e] += tv;
                         hit = hit || m;
                     }
                     if (!hit) {
-                        if (num < 4) {
+                        if (num < K) {
 #pragma unroll
-                            for (int e = 0; e < 4; e++)
+                            for (int e = 0; e < K; e++)
                                 if (e == num) {
                                     lid[e] = tid;
                                     v2[e] = tv;
@@ -343,21 +351,23 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
     }
     float lc[3];
     pf_partition_q(P, 0, pf_ld<CG>(sol + n * NSOL).x, ph_old, lc);
-    int pe[4];
-    float ce[4];
+    int pe[K];
+    float ce[K];
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
+    for (int e = 0; e < K; e++) {
         pe[e] = pf_lphase(lid[e], b1, b2);
         ce[e] = pe[e] == 1 ? lc[0] : (pe[e] == 2 ? lc[1] : lc[2]);
     }
     // Pair terms, each unordered pair once, in the order of pf_phase_cell.
-    float del[4] = {0.f, 0.f, 0.f, 0.f};
+    float del[K];
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
+    for (int e = 0; e < K; e++) del[e] = 0.f;
+#pragma unroll
+    for (int a = 0; a < K; a++) {
         if (a < num) {
             float da = del[a];
 #pragma unroll
-            for (int b = a + 1; b < 4; b++) {
+            for (int b = a + 1; b < K; b++) {
                 if (b < num) {
                     const int e = (pe[a] - 1) + 3 * (pe[b] - 1), ee = (pe[b] - 1) + 3 * (pe[a] - 1);
                     const float X = v2[a] * v1[b] - v2[b] * v1[a];
@@ -388,14 +398,14 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
             int mx = a, mid = lid[a];
             float mv = del[a];
 #pragma unroll
-            for (int b = a + 1; b < 4; b++)
+            for (int b = a + 1; b < K; b++)
                 if (b < num && del[b] > mv) {
                     mv = del[b];
                     mx = b;
                     mid = lid[b];
                 }
 #pragma unroll
-            for (int b = a + 1; b < 4; b++)
+            for (int b = a + 1; b < K; b++)
                 if (b == mx) {
                     del[b] = del[a];
                     lid[b] = lid[a];
