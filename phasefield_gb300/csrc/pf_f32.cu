@@ -51,6 +51,9 @@ __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__
     const int i = blockIdx.x * kPX + threadIdx.x;
     const int j = blockIdx.y * kPY + threadIdx.y;
     const int k = blockIdx.z;
+    __shared__ float4 coef[9];
+    pf_coef_table(P, coef);
+    __syncthreads();
     const unsigned plane = (unsigned)ix * (unsigned)iy;
     const unsigned n = (unsigned)i + (unsigned)ix * (unsigned)j + plane * (unsigned)k;
     bool defer = false;
@@ -62,7 +65,7 @@ __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__
         nb[3] = n + (unsigned)ix * (pf_wrap(j, iy, 1) - j);
         nb[4] = n + plane * (pf_wrap(k, iz, -1) - k);
         nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
-        defer = !pf_phase_cell_reg<NSOL>(P, n, nb, gid1, phi1, gid2, phi2, sphase, sol);
+        defer = !pf_phase_cell_reg<NSOL>(P, coef, n, nb, gid1, phi1, gid2, phi2, sphase, sol);
     }
     // One row of the block is one warp: every lane reaches the vote.
     pf_defer(defer, n, rest, rest_count);
@@ -81,6 +84,9 @@ __global__ void __launch_bounds__(kPT, 3) k_phase_f32_rest(const __grid_constant
                                                         const float2 *__restrict__ sol,
                                                         const unsigned int *__restrict__ rest,
                                                         const unsigned int *__restrict__ rest_count) {
+    __shared__ float4 coef[9];
+    pf_coef_table(P, coef);
+    __syncthreads();
     const unsigned cnt = *rest_count;
     const unsigned ix = (unsigned)P.ix, iy = (unsigned)P.iy, iz = (unsigned)P.iz;
     const unsigned plane = ix * iy;
@@ -95,7 +101,7 @@ __global__ void __launch_bounds__(kPT, 3) k_phase_f32_rest(const __grid_constant
         nb[3] = n + ix * (pf_wrap(j, (int)iy, 1) - j);
         nb[4] = n + plane * (pf_wrap(k, (int)iz, -1) - k);
         nb[5] = n + plane * (pf_wrap(k, (int)iz, 1) - k);
-        if (!pf_phase_cell_reg<NSOL, false, 8>(P, n, nb, gid1, phi1, gid2, phi2, sphase, sol)) {
+        if (!pf_phase_cell_reg<NSOL, false, 8>(P, coef, n, nb, gid1, phi1, gid2, phi2, sphase, sol)) {
             pf_plist<1> L;
             pf_phase_cell<NSOL, 1>(P, i, j, k, 0, gid1, phi1, gid2, phi2, sphase, sol, L);
         }

@@ -242,8 +242,20 @@ __device__ __forceinline__ void pf_phase_cell(const pf_f32_params &P, int i, int
 // hold (a (K+1)-th grain in the stencil, or own slots above the cutoff that
 // are not a prefix); the caller routes that cell to pf_phase_cell.  Cell indices
 // are 32-bit (grids of fewer than 2^32 cells).
+// The pair coefficients (A, B, G, E) of the nine phase pairs as one float4
+// each, for a shared-memory copy: a warp whose lanes need different pairs
+// reads them in one pass (indexed constant-bank loads serialise over the
+// distinct addresses of a warp).
+__device__ __forceinline__ void pf_coef_table(const pf_f32_params &P, float4 *tab) {
+    if (threadIdx.x + blockDim.x * threadIdx.y < 9) {
+        const int e = threadIdx.x + blockDim.x * threadIdx.y;
+        tab[e] = make_float4(P.A[e], P.B[e], P.G[e], P.E[e]);
+    }
+}
+
 template <int NSOL, bool CG = false, int K = 4>
-__device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsigned n, const unsigned nb[6],
+__device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, const float4 *__restrict__ coef,
+                                                  unsigned n, const unsigned nb[6],
                                                   const ushort4 *__restrict__ gid1,
                                                   const float4 *__restrict__ phi1, ushort4 *__restrict__ gid2,
                                                   float4 *__restrict__ phi2, float *__restrict__ sphase,
@@ -373,10 +385,11 @@ __device__ __forceinline__ bool pf_phase_cell_reg(const pf_f32_params &P, unsign
                     const float X = v2[a] * v1[b] - v2[b] * v1[a];
                     const float Y = v1[a] - v1[b];
                     const float Z = sqrtf(v1[a] * v1[b]);
-                    const float sym = P.A[e] * X + P.B[e] * Y;
+                    const float4 ce_ = coef[e], cee = coef[ee];
+                    const float sym = ce_.x * X + ce_.y * Y;
                     const float xa = P.dfmax ? fmaxf(ce[a], ce[b]) : ce[a], xb = P.dfmax ? fmaxf(ce[a], ce[b]) : ce[b];
-                    da += sym + P.G[e] * Z * (xa - P.E[e]);
-                    del[b] += -sym + P.G[ee] * Z * (xb - P.E[ee]);
+                    da += sym + ce_.z * Z * (xa - ce_.w);
+                    del[b] += -sym + cee.z * Z * (xb - cee.w);
                 }
             }
             float d = v1[a] + da;
