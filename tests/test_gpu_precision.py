@@ -72,3 +72,50 @@ def test_fp64_model_sensitivity_to_fp32_input(gpu, tmp_path):
     print(f"fp64 vs fp64(input rounded to fp32): max|dphase| {d.max():.3e}, cells > 1e-5: "
           f"{int((d.reshape(N, 3).max(1) > 1e-5).sum())}, fractions {fr}")
     assert np.all(fr <= 1e-6)
+
+
+@pytest.mark.parametrize("grid", [(32, 32, 16), (64, 48, 1)])
+def test_crowded_stencils_through_every_list_route(gpu, tmp_path, grid):
+    """Blocks of 8^3 (8^2 in 2D) cells each draw their grains from a pool of
+    five of their own, one to three per cell, so merged stencil lists of one
+    to four grains (register route), five to eight (the deferred register
+    route) and more (across block faces: the ten-entry list) all occur.  One
+    step against the FP64 four-slot model (the same algorithm): phase fields
+    within FP32 rounding (mean <= 1e-6; cells beyond 1e-4, where a clamp or
+    the top-four choice flips, under 0.5%)."""
+    m, _, spec = small_case(str(tmp_path), "3d256", grid, n_grains=3, n_nuclei=0, radius=2.0)
+    ix, iy, iz = grid
+    N = ix * iy * iz
+    rng = np.random.default_rng(7)
+    i, j, k = np.meshgrid(np.arange(ix), np.arange(iy), np.arange(iz), indexing="ij")
+    blk = ((i // 8) + (ix // 8) * ((j // 8) + (iy // 8) * (k // 8))).transpose(2, 1, 0).ravel()
+    ngr = rng.integers(1, 4, N)
+    ids = np.zeros((N, 6), np.int32)
+    phi = np.zeros((N, 6), np.float64)
+    for n in range(N):
+        members = rng.choice(5, ngr[n], replace=False)
+        v = np.sort(rng.uniform(0.05, 1.0, ngr[n]))[::-1]
+        # pool member 0..2 ferrite, 3..4 austenite; ids unique per block
+        g = np.where(members < 3, 100001 + 3 * blk[n] + members, 200001 + 2 * blk[n] + members - 3)
+        ids[n, :ngr[n]], phi[n, :ngr[n]] = g, v / v.sum()
+    phase = np.zeros((N, 3))
+    for sl in range(3):
+        p = ids[:, sl] // 100000
+        for q in (1, 2):
+            phase[:, q - 1] += np.where(p == q, phi[:, sl], 0.0)
+    C = np.concatenate([np.full(N, 0.1), np.full(N, 1.5)])
+    st = {"ids": ids.ravel(), "phi": phi.ravel(), "phase": phase.ravel(), "C": C}
+    A = pf.Adjoint(m, pf.PF_PREC_FP64, 1)
+    A.upload(st, 0.0)
+    A.forward(1)
+    ref = A.final_state()
+    A.close()
+    F = pf.PhaseField(m, pf.PF_PREC_FP32C)
+    F.upload(st, 0.0)
+    F.update(1)
+    got = F.download(conc=False)
+    F.close()
+    d = np.abs(got["phase"] - ref["phase"]).reshape(N, 3).max(1)
+    print(f"crowded {grid}: mean|dphase| {d.mean():.2e} max {d.max():.2e} cells > 1e-4: {(d > 1e-4).mean():.4f}")
+    assert d.mean() <= 1e-6
+    assert (d > 1e-4).mean() < 5e-3
