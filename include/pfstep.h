@@ -118,6 +118,11 @@ typedef struct {
      * driving force (Fortran_openmp_phase_field/PFM/src/sparse.f90:500-528,
      * 797-923), selected by a thermo file whose first word is F90_POLYNOMIAL. */
     int thermo_model;
+    /* 1: the driving force reads the phase concentrations averaged over the
+     * interface neighbourhood (Fortran model, sparse.f90:184-255; FP64 path
+     * only), selected by the keyword AVERAGED_INTERFACE_CARBON after
+     * F90_POLYNOMIAL in the thermo file. */
+    int avg_carbon;
 } pf_model;
 
 /* Per-step parameters evaluated on the host (Update_parameter,
@@ -141,6 +146,9 @@ typedef struct {
      * = -df_ratio_ij * (max(c_i, c_j) - df_ref) */
     int df_model;
     double df_ratio[9], df_ref;
+    /* > 0: half-width (i_intf + 1 cells) of the neighbourhood averaged for
+     * the driving force's phase concentrations; 0: the cell's own */
+    int avg_range;
 } pf_step_params;
 
 /* Seeded synthetic microstructure (replaces the reference's unseeded

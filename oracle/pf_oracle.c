@@ -156,6 +156,7 @@ void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
     p->diff_dt = m->dx * m->dx / maxD / p->dims * 0.2;
 
     p->df_model = 0;
+    p->avg_range = m->avg_carbon ? m->i_intf + 1 : 0; /* sparse.f90:186 */
     if (m->thermo_model == 1) {
         f90_thermo(T, p);
     } else {
@@ -230,7 +231,7 @@ static inline double driving_force(const pfo_params *p, int phii, int phjj, doub
 /* solver.cpp:147-304 (Phase_field_solver) for cell (i,j,k), 0-based. */
 static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, int k,
                        const int32_t *ids1, const double *phi1, int32_t *ids2, double *phi2,
-                       double *phase, double *conc1, const double *C) {
+                       double *phase, double *conc1, const double *C, const double *dfconc) {
     const int ix = m->ix, iy = m->iy, iz = m->iz;
     const long N = (long)ix * iy * iz;
     const long n = i + (long)ix * (j + (long)iy * k);
@@ -294,7 +295,7 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
     const double factor2 = PFO_PI * PFO_PI / (2. * p->eta * p->eta);
     const double factor3 = PFO_PI / p->eta;
     double local_conc[4];
-    for (int ii = 1; ii <= 3; ii++) local_conc[ii] = conc1[3 * n + ii - 1]; /* carbon */
+    for (int ii = 1; ii <= 3; ii++) local_conc[ii] = dfconc[3 * n + ii - 1]; /* carbon */
     for (int ii = 1; ii <= num; ii++) {
         const int gi = sid[ii], phi_ = sph[ii];
         (void)gi;
@@ -347,14 +348,92 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
         pfo_partition(C[q * N + n], phase + 3 * n, p->k[q], p->c[q], conc1 + q * 3 * N + 3 * n);
 }
 
+/* MYNGB (util_func.f90:33-47) restated 0-based: the cell n places away along
+ * an axis of length len, periodic. */
+static inline int f90_ngb(int c, int len, int n) {
+    int nn = n % len;
+    if (nn < 0) nn += len;
+    int r = c + nn;
+    if (r >= len) r -= len;
+    return r;
+}
+
+/* The Fortran model's interface-averaged phase concentrations for every
+ * cell (sparse.f90:141-146 and 184-255), from the phase fractions and phase
+ * concentrations of the start of the sweep (the Fortran loop reads values
+ * its own sweep may already have updated; here none are). */
+void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, const double *conc1,
+                  double *avg) {
+    const int ix = m->ix, iy = m->iy, iz = m->iz;
+    const double cutoff = m->cutoff;
+    const int R = p->avg_range;
+#define PH1(x, y, z) phase[3 * ((long)(x) + (long)ix * ((y) + (long)iy * (z)))]
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = 0; k < iz; k++)
+        for (int j = 0; j < iy; j++)
+            for (int i = 0; i < ix; i++) {
+                const long n = i + (long)ix * (j + (long)iy * k);
+                double out[3] = {conc1[3 * n], conc1[3 * n + 1], conc1[3 * n + 2]};
+                if (phase[3 * n] > cutoff && phase[3 * n + 1] > cutoff) { /* Flag_coexist(2) */
+                    double G[3];
+                    G[0] = PH1(f90_ngb(i, ix, 1), j, k) - PH1(f90_ngb(i, ix, -1), j, k);
+                    G[1] = PH1(i, f90_ngb(j, iy, 1), k) - PH1(i, f90_ngb(j, iy, -1), k);
+                    G[2] = PH1(i, j, f90_ngb(k, iz, 1)) - PH1(i, j, f90_ngb(k, iz, -1));
+                    for (int d = 0; d < 3; d++) G[d] = G[d] / 2.;
+                    double g2 = 0.;
+                    for (int d = 0; d < 3; d++) g2 += G[d] * G[d];
+                    const int rz = (iz - 1) / 2 < R ? (iz - 1) / 2 : R;
+                    const int ry = (iy - 1) / 2 < R ? (iy - 1) / 2 : R;
+                    const int rx = (ix - 1) / 2 < R ? (ix - 1) / 2 : R;
+                    double sum[3] = {0., 0., 0.}, num = 0.;
+                    for (int kk = -rz; kk <= rz; kk++) {
+                        const int z = f90_ngb(k, iz, kk);
+                        for (int jj = -ry; jj <= ry; jj++) {
+                            const int y = f90_ngb(j, iy, jj);
+                            for (int ii = -rx; ii <= rx; ii++) {
+                                const int x = f90_ngb(i, ix, ii);
+                                const double a = jj * G[2] - kk * G[1], b = kk * G[0] - ii * G[2],
+                                             c = ii * G[1] - jj * G[0];
+                                const double distance = a * a + b * b + c * c;
+                                if (distance > g2 * 1.0) continue;
+                                const long q = x + (long)ix * (y + (long)iy * z);
+                                const double p1 = phase[3 * q], p2 = phase[3 * q + 1];
+                                if (p1 < cutoff || p2 < cutoff) continue;
+                                const double h[3] = {PH1(f90_ngb(x, ix, 1), y, z) - PH1(f90_ngb(x, ix, -1), y, z),
+                                                     PH1(x, f90_ngb(y, iy, 1), z) - PH1(x, f90_ngb(y, iy, -1), z),
+                                                     PH1(x, y, f90_ngb(z, iz, 1)) - PH1(x, y, f90_ngb(z, iz, -1))};
+                                double dot = 0.;
+                                for (int d = 0; d < 3; d++) dot += G[d] * h[d];
+                                if (dot < 0.) continue;
+                                if (p1 < 0.4 * p2 || p1 > 2.5 * p2) continue;
+                                for (int d = 0; d < 3; d++) sum[d] += conc1[3 * q + d];
+                                num += 1.;
+                            }
+                        }
+                    }
+                    if (num > 0.)
+                        for (int d = 0; d < 3; d++) out[d] = sum[d] / num;
+                }
+                for (int d = 0; d < 3; d++) avg[3 * n + d] = out[d];
+            }
+#undef PH1
+}
+
 void pfo_phase_sweep(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phi1,
                      int32_t *ids2, double *phi2, double *phase, double *conc1, const double *C) {
+    double *avg = NULL;
+    if (p->avg_range > 0) {
+        const long N = (long)m->ix * m->iy * m->iz;
+        avg = (double *)malloc(3 * N * sizeof(double));
+        pfo_avg_conc(m, p, phase, conc1, avg);
+    }
     /* phase_field.cpp:252-257 */
 #pragma omp parallel for schedule(guided, 1) collapse(2)
     for (int k = 0; k < m->iz; k++)
         for (int j = 0; j < m->iy; j++)
             for (int i = 0; i < m->ix; i++)
-                phase_cell(m, p, i, j, k, ids1, phi1, ids2, phi2, phase, conc1, C);
+                phase_cell(m, p, i, j, k, ids1, phi1, ids2, phi2, phase, conc1, C, avg ? avg : conc1);
+    free(avg);
 }
 
 /* solver.cpp:343-372 (Diffusion_solver) for every solute */

@@ -51,6 +51,7 @@ typedef struct {
     double eq_a[9], eq_b[9], eq_c[9]; /* PARA functor a*T^2+b*T+c (thermo_functor.cpp:45-50) */
     double mn_ratio[3];           /* Mn partition ratios r_p: c_p = r_p * c_ref (solute 2 only) */
     int thermo_model;             /* 1: the Fortran model's polynomial thermodynamics (sparse.f90:797-923) */
+    int avg_carbon;               /* 1: interface-averaged concentrations in the driving force (sparse.f90:184-255) */
 } pfo_model;
 
 typedef struct {
@@ -66,6 +67,7 @@ typedef struct {
     double eta;
     int df_model;                 /* 1: driving force -ratio_ij*(max(c_i,c_j) - ref) (sparse.f90:512-515) */
     double df_ratio[9], df_ref;
+    int avg_range;                /* > 0: half-width of the averaged neighbourhood (i_intf + 1) */
 } pfo_params;
 
 typedef struct {
@@ -90,6 +92,9 @@ void pfo_partition_all(const pfo_model *m, const pfo_params *p, const double *ph
 /* solver.cpp:147-304 over all cells (phase_field.cpp:252-257) */
 void pfo_phase_sweep(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phi1,
                      int32_t *ids2, double *phi2, double *phase, double *conc1, const double *C);
+/* sparse.f90:184-255: interface-averaged phase concentrations of every cell */
+void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, const double *conc1,
+                  double *avg);
 /* solver.cpp:343-372 over all cells (phase_field.cpp:274-280) */
 void pfo_diffusion_substep(const pfo_model *m, const pfo_params *p, double dt_sub, const double *phase,
                            const double *conc1, double *conc2, double *C);

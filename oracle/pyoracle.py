@@ -39,6 +39,7 @@ class OModel(ctypes.Structure):
         ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
         ("mn_ratio", _d3),
         ("thermo_model", ctypes.c_int),
+        ("avg_carbon", ctypes.c_int),
     ]
 
 
@@ -55,6 +56,7 @@ class OParams(ctypes.Structure):
         ("dims", ctypes.c_double), ("eta", ctypes.c_double),
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
+        ("avg_range", ctypes.c_int),
     ]
 
 
@@ -88,6 +90,7 @@ def lib() -> ctypes.CDLL:
         L.pfo_params_at.restype = None
         L.pfo_partition_all.argtypes = [M, PP, _P, _P, _P]
         L.pfo_phase_sweep.argtypes = [M, PP, _P, _P, _P, _P, _P, _P, _P]
+        L.pfo_avg_conc.argtypes = [M, PP, _P, _P, _P]
         L.pfo_diffusion_substep.argtypes = [M, PP, _D, _P, _P, _P, _P]
         L.pfo_run.argtypes = [M, ctypes.POINTER(OState), ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.pfo_gpu_diffusion_solver.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -155,8 +158,15 @@ def parse_thermo(path: str, out: dict) -> None:
     for k in ("ent_a", "ent_b", "eq_a", "eq_b", "eq_c"):
         out[k] = [0.0] * 9
     out["thermo_model"] = 0
+    out["avg_carbon"] = 0
     if text.split()[:1] == ["F90_POLYNOMIAL"]:  # the Fortran model's built-in polynomials
         out["thermo_model"] = 1
+        for line in text.splitlines()[1:]:
+            words = line.split()
+            if words and not words[0].startswith("#"):
+                if words[0] != "AVERAGED_INTERFACE_CARBON":
+                    raise ValueError(f"thermo file: unknown keyword {words[0]}")
+                out["avg_carbon"] = 1
         return
     s = _Stream(text)
     s.ignore(3)
@@ -249,6 +259,7 @@ def model_from_dict(d: dict) -> OModel:
             arr[e] = v
     m.nsol = d["nsol"]
     m.thermo_model = d.get("thermo_model", 0)
+    m.avg_carbon = d.get("avg_carbon", 0)
     for q in range(2):
         for p in range(3):
             m.D0[q][p], m.DQ[q][p] = d["D0"][q][p], d["DQ"][q][p]
@@ -296,6 +307,13 @@ def partition_all(m: OModel, p: OParams, phase, C, conc) -> None:
 def phase_sweep(m: OModel, p: OParams, ids1, phi1, ids2, phi2, phase, conc1, C) -> None:
     lib().pfo_phase_sweep(ctypes.byref(m), ctypes.byref(p), _ptr(ids1), _ptr(phi1), _ptr(ids2), _ptr(phi2),
                           _ptr(phase), _ptr(conc1), _ptr(C))
+
+
+def avg_conc(m: OModel, p: OParams, phase, conc1) -> np.ndarray:
+    """The interface-averaged phase concentrations of every cell (sparse.f90:184-255)."""
+    out = np.zeros_like(conc1[: 3 * m.ix * m.iy * m.iz])
+    lib().pfo_avg_conc(ctypes.byref(m), ctypes.byref(p), _ptr(phase), _ptr(conc1), _ptr(out))
+    return out
 
 
 def diffusion_substep(m: OModel, p: OParams, dt_sub, phase, conc1, conc2, C) -> None:

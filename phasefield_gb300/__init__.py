@@ -67,6 +67,7 @@ class PfModel(ctypes.Structure):
         ("nple2_a", _d9), ("nple2_b", _d9), ("nple2_c", _d9),
         ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
         ("thermo_model", ctypes.c_int),
+        ("avg_carbon", ctypes.c_int),
     ]
 
 
@@ -88,6 +89,7 @@ class PfStepParams(ctypes.Structure):
         ("k", _d9 * 2), ("c", _d9 * 2),
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
+        ("avg_range", ctypes.c_int),
     ]
 
 

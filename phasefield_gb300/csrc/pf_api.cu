@@ -129,6 +129,7 @@ struct pf_ctx {
     double *phase = nullptr;
     double *conc[2] = {nullptr, nullptr};
     double *C = nullptr;
+    double *avg = nullptr;  // interface-averaged concentrations (models with avg_carbon)
     int cur = 0, curc = 0;
     // FP32 compact layout
     ushort4 *gid[2] = {nullptr, nullptr};
@@ -223,7 +224,7 @@ void free_all(pf_ctx *c) {
         cudaFree(c->ids[i]); cudaFree(c->phi[i]); cudaFree(c->conc[i]);
         cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
     }
-    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->phase32);
+    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->avg); cudaFree(c->phase32);
     cudaFree(c->d_span); cudaFree(c->d_trunc); cudaFree(c->rest); cudaFree(c->rest_count);
     cudaFree(c->st_ids); cudaFree(c->st_phi); cudaFree(c->st_phase); cudaFree(c->st_C); cudaFree(c->st_conc);
     cudaFree(c->partials); cudaFree(c->d_red);
@@ -242,7 +243,7 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         const int a = c->cur;
         e = timed(c, 0, [&] {
             return pf_launch_phase_f64(P, c->ids[a], c->phi[a], c->ids[1 - a], c->phi[1 - a], c->phase,
-                                       c->conc[c->curc], c->C, c->stream);
+                                       c->conc[c->curc], c->C, c->avg, c->stream);
         });
         if (e != cudaSuccess) return e;
         c->cur = 1 - a;
@@ -350,6 +351,8 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         return pf_fail(PF_ERR_ARG, "pf_create: bad model");
     if (precision == PF_PREC_FP32C && (long long)model->ix * model->iy * model->iz > 0xffffffffLL)
         return pf_fail(PF_ERR_RANGE, "pf_create: the compact FP32 path indexes cells with 32 bits");
+    if (precision == PF_PREC_FP32C && model->avg_carbon)
+        return pf_fail(PF_ERR_ARG, "pf_create: the interface-averaged carbon runs on the FP64 path only");
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
         cudaGetLastError();
@@ -376,6 +379,7 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         }
         alloc((void **)&c->phase, 3 * N * sizeof(double));
         alloc((void **)&c->C, N * c->nsol * sizeof(double));
+        if (model->avg_carbon) alloc((void **)&c->avg, 3 * N * sizeof(double));
     } else {
         for (int i = 0; i < 2; i++) {
             alloc((void **)&c->gid[i], N * sizeof(ushort4));
@@ -794,6 +798,7 @@ extern "C" int pf_batch_create(const pf_model *models, int ndom, pf_batch **out)
         const pf_model &m = models[d];
         if (m.iz != 1) return pf_fail(PF_ERR_ARG, "pf_batch_create: batched domains are 2D (iz == 1)");
         if (m.nsol != models[0].nsol) return pf_fail(PF_ERR_ARG, "pf_batch_create: all domains need the same solutes");
+        if (m.avg_carbon) return pf_fail(PF_ERR_ARG, "pf_batch_create: the interface-averaged carbon runs on the FP64 path only");
         for (int t = 1; t < m.nT; t++)
             if (m.T_temp[t] != m.T_temp[0])
                 return pf_fail(PF_ERR_ARG, "pf_batch_create: each domain needs a constant temperature");

@@ -12,6 +12,12 @@ __device__ __forceinline__ int pf_wrap(int i, int len, int d) {
     return g;
 }
 
+// v mod L in [0, L) for any int v.
+__device__ __forceinline__ int pf_mod(int v, int L) {
+    v %= L;
+    return v < 0 ? v + L : v;
+}
+
 // phase_field.h:25-29: grain id -> phase (0 for an empty slot).
 __device__ __forceinline__ int pf_phase_of_grain(int g) {
     if (g == 0) return 0;

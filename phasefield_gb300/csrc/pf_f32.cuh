@@ -34,10 +34,6 @@ __device__ __forceinline__ void pf_partition_q(const pf_f32_params &P, int q, fl
     }
 }
 
-__device__ __forceinline__ int pf_mod(int v, int L) {
-    v %= L;
-    return v < 0 ? v + L : v;
-}
 
 // The list storage of the phase sweep: one column per thread, PF_NSTENCIL
 // entries (grain id, own phi, neighbour phi sum, updated value).

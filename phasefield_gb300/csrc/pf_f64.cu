@@ -44,14 +44,93 @@ __device__ __forceinline__ void pf_partition(double C, const double ph[3], const
     }
 }
 
-// Phase_field_solver (solver.cpp:147-304), one thread per cell.
+// The Fortran model's interface-averaged phase concentrations
+// (sparse.f90:184-255), one thread per cell, from the phase fractions and
+// phase concentrations before the sweep.  In a cell holding ferrite and
+// austenite above the cutoff (Flag_coexist(2), sparse.f90:141-146) the
+// average runs over the cells of the (2R+1)^dims neighbourhood (R = i_intf+1,
+// clipped to half the grid) that lie within one cell of the line through
+// the cell along G = grad(phi_ferrite)/2 (|r x G|^2 <= |G|^2), hold both
+// phases above the cutoff, whose own ferrite gradient does not point against
+// G, and whose ferrite/austenite ratio lies in [0.4, 2.5]; with no such cell,
+// and elsewhere, the cell's own concentrations.  The Fortran loop updates the
+// phase fractions in place as it goes (an order the OpenMP schedule decides);
+// here every cell reads the values of the start of the sweep.
+__global__ void __launch_bounds__(256) k_avg_conc_f64(const __grid_constant__ pf_step_params P,
+                                                      const double *__restrict__ phase,
+                                                      const double *__restrict__ conc1,
+                                                      double *__restrict__ avg) {
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
+    const int ix = P.ix, iy = P.iy, iz = P.iz;
+    const double cutoff = P.cutoff;
+    double out[3] = {conc1[3 * n], conc1[3 * n + 1], conc1[3 * n + 2]};
+    auto at = [&](int i, int j, int k) { return (long long)i + (long long)ix * (j + (long long)iy * k); };
+    auto ph1 = [&](int i, int j, int k) { return phase[3 * at(i, j, k)]; };
+    if (phase[3 * n] > cutoff && phase[3 * n + 1] > cutoff) {
+        double G[3];
+        G[0] = ph1(pf_wrap(ci, ix, 1), cj, ck) - ph1(pf_wrap(ci, ix, -1), cj, ck);
+        G[1] = ph1(ci, pf_wrap(cj, iy, 1), ck) - ph1(ci, pf_wrap(cj, iy, -1), ck);
+        G[2] = ph1(ci, cj, pf_wrap(ck, iz, 1)) - ph1(ci, cj, pf_wrap(ck, iz, -1));
+        G[0] = G[0] / 2.; G[1] = G[1] / 2.; G[2] = G[2] / 2.;
+        double g2 = 0.;
+        g2 += G[0] * G[0];
+        g2 += G[1] * G[1];
+        g2 += G[2] * G[2];
+        const int R = P.avg_range;
+        const int rz = min((iz - 1) / 2, R), ry = min((iy - 1) / 2, R), rx = min((ix - 1) / 2, R);
+        double sum[3] = {0., 0., 0.}, num = 0.;
+        for (int kk = -rz; kk <= rz; kk++) {
+            const int z = pf_mod(ck + kk, iz);
+            for (int jj = -ry; jj <= ry; jj++) {
+                const int y = pf_mod(cj + jj, iy);
+                for (int ii = -rx; ii <= rx; ii++) {
+                    const int x = pf_mod(ci + ii, ix);
+                    const double a = jj * G[2] - kk * G[1], b = kk * G[0] - ii * G[2], c = ii * G[1] - jj * G[0];
+                    const double dist = a * a + b * b + c * c;
+                    if (dist > g2 * 1.0) continue;
+                    const long long m = at(x, y, z);
+                    const double p1 = phase[3 * m], p2 = phase[3 * m + 1];
+                    if (p1 < cutoff || p2 < cutoff) continue;
+                    const double h0 = ph1(pf_wrap(x, ix, 1), y, z) - ph1(pf_wrap(x, ix, -1), y, z);
+                    const double h1 = ph1(x, pf_wrap(y, iy, 1), z) - ph1(x, pf_wrap(y, iy, -1), z);
+                    const double h2 = ph1(x, y, pf_wrap(z, iz, 1)) - ph1(x, y, pf_wrap(z, iz, -1));
+                    double dot = 0.;
+                    dot += G[0] * h0;
+                    dot += G[1] * h1;
+                    dot += G[2] * h2;
+                    if (dot < 0.) continue;
+                    if (p1 < 0.4 * p2 || p1 > 2.5 * p2) continue;
+                    sum[0] += conc1[3 * m];
+                    sum[1] += conc1[3 * m + 1];
+                    sum[2] += conc1[3 * m + 2];
+                    num += 1.;
+                }
+            }
+        }
+        if (num > 0.) {
+            out[0] = sum[0] / num;
+            out[1] = sum[1] / num;
+            out[2] = sum[2] / num;
+        }
+    }
+    avg[3 * n] = out[0];
+    avg[3 * n + 1] = out[1];
+    avg[3 * n + 2] = out[2];
+}
+
+// Phase_field_solver (solver.cpp:147-304), one thread per cell.  avg (may be
+// null): the phase concentrations the driving force reads instead of the
+// cell's own (k_avg_conc_f64).
 __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P,
                                                    const int *__restrict__ ids1,
                                                    const double *__restrict__ phi1,
                                                    int *__restrict__ ids2, double *__restrict__ phi2,
                                                    double *__restrict__ phase,
                                                    double *__restrict__ conc1,
-                                                   const double *__restrict__ C) {
+                                                   const double *__restrict__ C,
+                                                   const double *__restrict__ avg) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
@@ -149,8 +228,9 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
     // Driving forces depend only on the phase pair and the cell's carbon
     // concentration (solver.cpp:231-232, 374-387): evaluate the six ordered
     // off-diagonal pairs once.
+    const double *lcp = avg ? avg : conc1;
     double lc[3];
-    lc[0] = conc1[3 * n + 0]; lc[1] = conc1[3 * n + 1]; lc[2] = conc1[3 * n + 2];
+    lc[0] = lcp[3 * n + 0]; lc[1] = lcp[3 * n + 1]; lc[2] = lcp[3 * n + 2];
     double df[9];
 #pragma unroll
     for (int a = 1; a <= 3; a++)
@@ -328,9 +408,16 @@ inline unsigned pf_blocks(long long N, int threads) { return (unsigned)((N + thr
 }  // namespace
 
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
-                                double *phi2, double *phase, double *conc1, const double *C,
+                                double *phi2, double *phase, double *conc1, const double *C, double *avg,
                                 cudaStream_t s) {
-    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C);
+    const bool averaged = P.avg_range > 0 && avg;
+    if (averaged) {
+        k_avg_conc_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, phase, conc1, avg);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C,
+                                                                           averaged ? avg : nullptr);
     return cudaGetLastError();
 }
 

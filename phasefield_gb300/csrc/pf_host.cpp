@@ -73,11 +73,22 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
         m->eq_a[e] = m->eq_b[e] = m->eq_c[e] = 0.;
     }
     m->thermo_model = 0;
+    m->avg_carbon = 0;
     {
         std::string word;
         f >> word;
         if (word == "F90_POLYNOMIAL") {  // every coefficient is built in (pf_f90_thermo)
             m->thermo_model = 1;
+            // Optional keywords on the following lines ('#' starts a comment line).
+            std::string line;
+            std::getline(f, line);
+            while (std::getline(f, line)) {
+                std::istringstream ls(line);
+                std::string kw;
+                if (!(ls >> kw) || kw[0] == '#') continue;
+                if (kw == "AVERAGED_INTERFACE_CARBON") m->avg_carbon = 1;
+                else return pf_fail(PF_ERR_IO, "thermo file: unknown keyword " + kw);
+            }
             return PF_OK;
         }
         f.clear();
@@ -343,6 +354,7 @@ void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
         }
     p.pfm_dt = m.dx * m.dx / dims * 0.2 / maxms;
     p.diff_dt = m.dx * m.dx / maxD / dims * 0.2;
+    p.avg_range = m.avg_carbon ? m.i_intf + 1 : 0;  // sparse.f90:186
     if (m.thermo_model == 1) {
         pf_f90_thermo(T, p);
     } else {

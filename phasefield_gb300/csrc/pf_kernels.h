@@ -4,8 +4,10 @@
 #include "pf_types.h"
 
 // ---- FP64 reference layout (pf_f64.cu) ----
+// avg: 3N doubles of scratch for the interface-averaged concentrations
+// (used when P.avg_range > 0; may be null otherwise).
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
-                                double *phi2, double *phase, double *conc1, const double *C,
+                                double *phi2, double *phase, double *conc1, const double *C, double *avg,
                                 cudaStream_t s);
 cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
                                   const double *conc1, double *conc2, double *C, cudaStream_t s);

@@ -76,8 +76,13 @@ THERMO_F90_TEXT = """F90_POLYNOMIAL
 
 
 def write_thermo(path: str, model: str = "linear") -> str:
+    """model: "linear" (the reference's sample lines), "f90" (the Fortran
+    model's thermodynamics) or "f90avg" (that, plus the interface-averaged
+    carbon of sparse.f90:184-255)."""
+    text = {"linear": THERMO_TEXT, "f90": THERMO_F90_TEXT,
+            "f90avg": THERMO_F90_TEXT + "AVERAGED_INTERFACE_CARBON\n"}[model]
     with open(path, "w") as f:
-        f.write(THERMO_F90_TEXT if model == "f90" else THERMO_TEXT)
+        f.write(text)
     return path
 
 

@@ -102,3 +102,102 @@ def test_adjoint_rejects_f90_thermodynamics(tmp_path):
     cfg, m, om = _case(str(tmp_path))
     h = pf.ctypes.c_void_p()
     assert pf.lib().pf_adj_create(pf.ctypes.byref(m), pf.PF_PREC_FP64, 10, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
+
+
+def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf):
+    """sparse.f90:141-146 and 184-255 written out literally (1-based indices,
+    MYNGB of util_func.f90:33-47), on the values of the start of the sweep."""
+    ix, iy, iz = grid
+    ph = phase.reshape(iz, iy, ix, 3)
+    cc = conc.reshape(iz, iy, ix, 3)
+    out = cc.copy()
+
+    def myngb(coord, lcoord, n):
+        nn = n % lcoord
+        r = coord + nn
+        return r - lcoord if r > lcoord else (r + lcoord if r < 1 else r)
+
+    def vp(p, i, j, k):  # Val_phase(p, i, j, k), 1-based
+        return ph[k - 1, j - 1, i - 1, p - 1]
+
+    rng_ = i_intf + 1
+    for K in range(1, iz + 1):
+        for J in range(1, iy + 1):
+            for I in range(1, ix + 1):
+                if not (vp(1, I, J, K) > cutoff and vp(2, I, J, K) > cutoff):
+                    continue
+                grad = [vp(1, myngb(I, ix, 1), J, K) - vp(1, myngb(I, ix, -1), J, K),
+                        vp(1, I, myngb(J, iy, 1), K) - vp(1, I, myngb(J, iy, -1), K),
+                        vp(1, I, J, myngb(K, iz, 1)) - vp(1, I, J, myngb(K, iz, -1))]
+                grad = [g / 2. for g in grad]
+                g2 = 0.
+                for g in grad:
+                    g2 += g * g
+                num, acc = 0., [0., 0., 0.]
+                for Kk in range(-min((iz - 1) // 2, rng_), min((iz - 1) // 2, rng_) + 1):
+                    Iiz = myngb(K, iz, Kk)
+                    for Jj in range(-min((iy - 1) // 2, rng_), min((iy - 1) // 2, rng_) + 1):
+                        Iiy = myngb(J, iy, Jj)
+                        for Ii in range(-min((ix - 1) // 2, rng_), min((ix - 1) // 2, rng_) + 1):
+                            Iix = myngb(I, ix, Ii)
+                            a = Jj * grad[2] - Kk * grad[1]
+                            b = Kk * grad[0] - Ii * grad[2]
+                            c = Ii * grad[1] - Jj * grad[0]
+                            if a * a + b * b + c * c > g2 * 1.0:
+                                continue
+                            if vp(1, Iix, Iiy, Iiz) < cutoff or vp(2, Iix, Iiy, Iiz) < cutoff:
+                                continue
+                            h = [vp(1, myngb(Iix, ix, 1), Iiy, Iiz) - vp(1, myngb(Iix, ix, -1), Iiy, Iiz),
+                                 vp(1, Iix, myngb(Iiy, iy, 1), Iiz) - vp(1, Iix, myngb(Iiy, iy, -1), Iiz),
+                                 vp(1, Iix, Iiy, myngb(Iiz, iz, 1)) - vp(1, Iix, Iiy, myngb(Iiz, iz, -1))]
+                            dot = 0.
+                            for d in range(3):
+                                dot += grad[d] * h[d]
+                            if dot < 0.:
+                                continue
+                            p1, p2 = vp(1, Iix, Iiy, Iiz), vp(2, Iix, Iiy, Iiz)
+                            if p1 < 0.4 * p2 or p1 > 2.5 * p2:
+                                continue
+                            for d in range(3):
+                                acc[d] += cc[Iiz - 1, Iiy - 1, Iix - 1, d]
+                            num += 1.
+                if num > 0.:
+                    out[K - 1, J - 1, I - 1] = [a_ / num for a_ in acc]
+    return out.ravel()
+
+
+@pytest.mark.parametrize("grid", [(24, 20, 1), (10, 9, 8)])
+def test_averaged_interface_carbon_oracle_equals_fortran_literal(tmp_path, grid):
+    W.write_thermo(str(tmp_path / "thermo_avg.txt"), "f90avg")
+    cfg = W.write_config(str(tmp_path / "avg.txt"), grid=grid, T=1023.0, thermo_file="thermo_avg.txt",
+                         directory=str(tmp_path / "out"))
+    m, om = pf.read_model(cfg), po.load_model(cfg)
+    assert m.avg_carbon == 1 and om.avg_carbon == 1
+    assert pf.params_at(m, 0.0).avg_range == m.i_intf + 1 == po.params_at(om, 0.0).avg_range
+    spec = W.WORKLOADS["3d256"].spec()
+    spec.n_grains, spec.n_nuclei, spec.nucleus_radius = 3, 4, 2.5
+    st = po.init_state(om, spec, 0.0)
+    p = po.params_at(om, 0.0)
+    N = grid[0] * grid[1] * grid[2]
+    conc = np.zeros(3 * N * om.nsol)
+    po.partition_all(om, p, st["phase"], st["C"], conc)
+    conc = conc[: 3 * N] + 1e-3 * np.sin(np.arange(3 * N))  # distinct values per cell
+    got = po.avg_conc(om, p, st["phase"], conc)
+    want = _avg_fortran_literal(st["phase"], conc, grid, om.cutoff, om.i_intf)
+    assert np.array_equal(got, want)
+    assert not np.array_equal(got, conc)  # the averaging changed some cells
+
+
+def test_averaged_carbon_keyword_and_precision_checks(tmp_path):
+    with open(tmp_path / "bad.txt", "w") as f:
+        f.write("F90_POLYNOMIAL\nNO_SUCH_OPTION\n")
+    cfg = W.write_config(str(tmp_path / "bad_cfg.txt"), grid=(8, 8, 1), thermo_file="bad.txt",
+                         directory=str(tmp_path / "out"))
+    with pytest.raises(pf.PfError):
+        pf.read_model(cfg)
+    W.write_thermo(str(tmp_path / "thermo_avg.txt"), "f90avg")
+    cfg = W.write_config(str(tmp_path / "avg.txt"), grid=(8, 8, 1), thermo_file="thermo_avg.txt",
+                         directory=str(tmp_path / "out"))
+    m = pf.read_model(cfg)
+    h = pf.ctypes.c_void_p()
+    assert pf.lib().pf_create(pf.ctypes.byref(m), pf.PF_PREC_FP32C, pf.ctypes.byref(h)) == pf.PF_ERR_ARG

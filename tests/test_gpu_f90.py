@@ -47,3 +47,34 @@ def test_f90_fp64_matches_oracle(gpu, tmp_path, grid, T):
     G.upload(st0, 0.0)
     G.update(1)
     np.testing.assert_allclose(G.fractions()[:3], F.fractions()[:3], atol=1e-3)
+
+
+@pytest.mark.parametrize("grid", [(48, 40, 1), (16, 14, 12)])
+def test_f90_averaged_carbon_fp64_matches_oracle(gpu, tmp_path, grid):
+    """The interface-averaged carbon (sparse.f90:184-255) on the FP64 path:
+    every field bit for bit equal to the oracle after six steps."""
+    W.write_thermo(str(tmp_path / "thermo_avg.txt"), "f90avg")
+    cfg = W.write_config(str(tmp_path / "avg.txt"), grid=grid, T=1023.0, thermo_file="thermo_avg.txt",
+                         directory=str(tmp_path / "out"))
+    m, om = pf.read_model(cfg), po.load_model(cfg)
+    spec = W.WORKLOADS["3d256"].spec()
+    spec.n_grains, spec.n_nuclei, spec.nucleus_radius = 4, 5, 3.0
+    st0 = pf.init_microstructure(m, spec, 0.0)
+    ref = copy_state(st0)
+    t_ref = po.run(om, ref, 0.0, 6)
+    F = pf.PhaseField(m, pf.PF_PREC_FP64)
+    F.upload(st0, 0.0)
+    F.update(6)
+    got = F.download()
+    F.close()
+    assert got["time"] == t_ref
+    assert np.array_equal(got["ids"], ref["ids"])
+    for k in ("phi", "phase", "conc", "C"):
+        assert np.array_equal(got[k], ref[k]), k
+    # the averaging is in effect: the same steps without it end elsewhere
+    plain = copy_state(st0)
+    W.write_thermo(str(tmp_path / "thermo_f90.txt"), "f90")
+    cfg2 = W.write_config(str(tmp_path / "f90.txt"), grid=grid, T=1023.0, thermo_file="thermo_f90.txt",
+                          directory=str(tmp_path / "out"))
+    po.run(po.load_model(cfg2), plain, 0.0, 6)
+    assert not np.array_equal(plain["phi"], ref["phi"])
