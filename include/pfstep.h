@@ -123,6 +123,12 @@ typedef struct {
      * only), selected by the keyword AVERAGED_INTERFACE_CARBON after
      * F90_POLYNOMIAL in the thermo file. */
     int avg_carbon;
+    /* 1: the Fortran model's Purdy-Brechet solute drag on ferrite/austenite
+     * interfaces (sparse.f90:326-360, 538-671, 958-1041; FP64 path only),
+     * selected by "SOLUTE_DRAG binding_energy v_max0 q_sd" after
+     * F90_POLYNOMIAL in the thermo file (J/mol, um/s, J/mol). */
+    int drag;
+    double drag_binding, drag_vmax0, drag_qsd;
 } pf_model;
 
 /* Per-step parameters evaluated on the host (Update_parameter,
@@ -149,6 +155,13 @@ typedef struct {
     /* > 0: half-width (i_intf + 1 cells) of the neighbourhood averaged for
      * the driving force's phase concentrations; 0: the cell's own */
     int avg_range;
+    /* Solute drag at the step's temperature (PARAMETER_DRAG_PB,
+     * sparse.f90:958-1003): v_max, E0 = binding/RT, the Mn segregation
+     * parameters of heating / cooling and the bulk fraction of the first
+     * species, the correction factors and zero-velocity drags [heating, cooling]. */
+    int drag_model;
+    double drag_vmax, drag_ex0, drag_de_heat, drag_de_cool, drag_u0;
+    double drag_corr[2], drag_drag0[2];
 } pf_step_params;
 
 /* Seeded synthetic microstructure (replaces the reference's unseeded

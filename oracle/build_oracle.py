@@ -48,7 +48,11 @@ REPO = os.path.dirname(HERE)
 # the CPU baseline steps exactly the state the GPU steps (it generates inputs;
 # it is not part of what is checked).
 INIT_SRC = os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init.cpp")
-INIT_HDRS = [os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init.h"), os.path.join(REPO, "include", "pfstep.h")]
+INIT_HDRS = [os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init.h"), os.path.join(REPO, "include", "pfstep.h"),
+             os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init_cell.h"),
+             os.path.join(REPO, "phasefield_gb300", "csrc", "pf_init_setup.h"),
+             # exp/log shared with the product so the solute-drag bisection rounds alike
+             os.path.join(REPO, "phasefield_gb300", "csrc", "pf_math.h")]
 
 
 def build_oracle(force: bool = False) -> str:
@@ -58,8 +62,8 @@ def build_oracle(force: bool = False) -> str:
         o1 = os.path.join(BUILD, "pf_oracle.o")
         o2 = os.path.join(BUILD, "pf_init.o")
         inc = ["-I", os.path.join(REPO, "include"), "-I", os.path.join(REPO, "phasefield_gb300", "csrc")]
-        cmds = [["gcc", "-O3", "-std=c99", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-c", src[0],
-                 "-o", o1],
+        cmds = [["gcc", "-O3", "-std=c99", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"] + inc +
+                ["-c", src[0], "-o", o1],
                 ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"] + inc +
                 ["-c", INIT_SRC, "-o", o2],
                 ["g++", "-shared", "-fopenmp", o1, o2, "-o", LIB, "-lm"]]

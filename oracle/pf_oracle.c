@@ -10,6 +10,10 @@
  */
 #include "pf_oracle.h"
 #include <math.h>
+
+#include "pf_math.h" /* exp/log shared with the product's GPU kernel (identical rounding) */
+
+int pfo_drag_failures; /* set when a solute-drag iteration finds no root (the Fortran stops) */
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -133,6 +137,123 @@ static void f90_thermo(double T, pfo_params *p) {
     p->df_model = 1;
 }
 
+/* SOLUTE_DRAG_PB (sparse.f90:1005-1037), literally. */
+static double f90_solute_drag_pb(double V0, double E0, double De, double U0, double V_max, double Temperature) {
+    const double V = V0 / V_max;
+    const double A = (De - E0) + V;
+    const double B = (De + E0) + V;
+    const double D0 = 1. - U0;
+    const double Vu0 = V * U0;
+    const double D1_d0 = (A - Vu0) / (A * D0 + (A - V) * U0 * pf_exp(-(A - Vu0)));
+    const double D1 = D0 * D1_d0;
+    const double U1 = 1. - D1;
+    const double D2_d1 = (B - Vu0) / (B * D1 + (B * U1 - Vu0) * pf_exp(-(B - Vu0)));
+    return (2. * De * U0 - ((A - V) / A * (Vu0 + pf_log(D1_d0)) + (B - V) / B * (Vu0 + pf_log(D2_d1)))) * 8.314 *
+           Temperature / 7.2e12;
+}
+
+/* DISSIPATION_ITERATION (sparse.f90:538-605; heating) and _R (607-660;
+ * cooling), literally; Solution enters with the caller's value and keeps it
+ * when no bracket is found (the _R variant stops the Fortran program there:
+ * counted in pfo_drag_failures).  The bisection gets a limit of 200 halvings
+ * the Fortran loop lacks (reached only for a root at exactly zero). */
+static double f90_dissipation(double Solution, double Driv, double Drag, double Norm, int heating,
+                              const pfo_params *p) {
+    const double drag0 = heating ? p->drag_drag0[0] : p->drag_drag0[1];
+    const double De = heating ? p->drag_de_heat : p->drag_de_cool;
+    const double Cf = heating ? p->drag_corr[0] : p->drag_corr[1];
+    double Err1, Err2 = Driv - Drag * drag0, Dv, V, X1, X2, Tmp_v, Tmp_err;
+    if (Err2 < 0.) return 0.;
+    Dv = 0.1 * p->drag_vmax;
+    V = 0.;
+    for (int J = 1; J <= 2; J++) {
+        for (int I = 1; I <= 40; I++) {
+            Err1 = Err2;
+            V = V + Dv;
+            Err2 = Driv - V * Norm - Drag * (f90_solute_drag_pb(V, p->drag_ex0, De, p->drag_u0, p->drag_vmax, p->T) * Cf);
+            if (Err1 * Err2 <= 0.) {
+                X1 = V - Dv;
+                X2 = V;
+                int it = 0;
+                while ((X2 - X1) > 0.01 * X2) {
+                    if (++it > 200) {
+                        pfo_drag_failures = 1;
+                        break;
+                    }
+                    Tmp_v = 0.5 * (X1 + X2);
+                    Tmp_err = Driv - Tmp_v * Norm -
+                              Drag * (f90_solute_drag_pb(Tmp_v, p->drag_ex0, De, p->drag_u0, p->drag_vmax, p->T) * Cf);
+                    if (Err1 * Tmp_err <= 0.) {
+                        X2 = Tmp_v;
+                        Err2 = Tmp_err;
+                    } else {
+                        X1 = Tmp_v;
+                        Err1 = Tmp_err;
+                    }
+                }
+                return 0.5 * (X1 + X2) * Norm;
+            }
+        }
+        V = Driv / Norm;
+        Dv = -0.2 * V;
+        Err2 = -1.;
+    }
+    if (!heating) pfo_drag_failures = 1;
+    return Solution;
+}
+
+/* The shared exp/log, exported so the tests can check them against the C
+ * library and against the GPU build. */
+double pfo_exp(double x) { return pf_exp(x); }
+double pfo_log(double x) { return pf_log(x); }
+
+/* PARAMETER_DRAG_PB (sparse.f90:958-1003) restated: V_max, M_nple, N_nple,
+ * Ux0, De_heat, De_cool, Ex0, Driv_f (with Ref_c_nple(2,1) and
+ * Ref_c_nple_r(2,1) of THERMO_DATA, sparse.f90:844-880; the latter stays at
+ * its initial 0 below 1041.3 K), Drag0 and Correct_factor.  exp/log are
+ * pf_exp/pf_log, as in the product, so both round alike. */
+static double f90_max(double a, double b) { return a > b ? a : b; }
+static void f90_drag(const pfo_model *m, double T, pfo_params *p) {
+    p->drag_vmax = m->drag_vmax0 * pf_exp(-m->drag_qsd / (8.314 * T));
+    const double x = T - 273.15;
+    double M_nple[3], N_nple[3];
+    M_nple[0] = f90_max(1.E-10, 3.9793e-5 * x - 2.3163e-2);
+    M_nple[1] = f90_max(1.E-10, -2.928e-8 * (x * x) + 5.629e-5 * x - 2.35e-2);
+    M_nple[2] = f90_max(1.E-10, 2.253e-8 * (x * x) - 4.255e-5 * x + 2.351e-2);
+    N_nple[0] = f90_max(1.E-10, -3.818e-9 * (x * x * x) + 9.055e-6 * (x * x) - 7.408e-3 * x + 2.118);
+    N_nple[1] = f90_max(1.E-10, -7.1227e-10 * (x * x * x) + 1.6307e-6 * (x * x) - 1.2584e-3 * x + 3.3166e-1);
+    N_nple[2] = 3.E-3;
+    const double Ux0[3] = {1.887e-2, 3.65e-3, 3.12e-3};
+    double De_heat[3], De_cool[3];
+    for (int i = 0; i < 3; i++) {
+        De_heat[i] = -0.5 * pf_log(M_nple[i] * (1. - Ux0[i]) / (Ux0[i] * (1. - M_nple[i])));
+        De_cool[i] = -0.5 * pf_log(N_nple[i] * (1. - Ux0[i]) / (Ux0[i] * (1. - N_nple[i])));
+    }
+    const double Ex0 = m->drag_binding / (8.314 * T);
+    const double ref_nple21 = T < 1110.64 ? f90_poly4(T - 1110.64, -3.3441e-3, 1.0406e-5, -5.6345e-8, 0.0)
+                                          : f90_poly4(T - 1110.64, -3.23154e-3, 0., 0., 0.);
+    const double ref_nple_r21 = T < 1041.3 ? 0. : -2.39e-3 * (T - 1041.3);
+    const double Driv_f1 = fabs(M3(p->df_ratio, 2, 1) * (M3(p->eq, 2, 1) - ref_nple21));
+    const double Driv_f2 = fabs(M3(p->df_ratio, 2, 1) * (M3(p->eq, 2, 1) - ref_nple_r21));
+    const double vm = p->drag_vmax;
+    double Drag0_1 = f90_solute_drag_pb(0., Ex0, De_heat[0], Ux0[0], vm, T) + f90_solute_drag_pb(0., 0., De_heat[1], Ux0[1], vm, T) +
+                     f90_solute_drag_pb(0., 0., De_heat[2], Ux0[2], vm, T);
+    double Drag0_2 = f90_solute_drag_pb(0., Ex0, De_cool[0], Ux0[0], vm, T) + f90_solute_drag_pb(0., 0., De_cool[1], Ux0[1], vm, T) +
+                     f90_solute_drag_pb(0., 0., De_cool[2], Ux0[2], vm, T);
+    const double Correct_factor1 = Driv_f1 / Drag0_1, Correct_factor2 = Driv_f2 / Drag0_2;
+    Drag0_1 = f90_solute_drag_pb(0., Ex0, De_heat[0], Ux0[0], vm, T) * Correct_factor1;
+    Drag0_2 = f90_solute_drag_pb(0., Ex0, De_cool[0], Ux0[0], vm, T) * Correct_factor2;
+    p->drag_ex0 = Ex0;
+    p->drag_de_heat = De_heat[0];
+    p->drag_de_cool = De_cool[0];
+    p->drag_u0 = Ux0[0];
+    p->drag_corr[0] = Correct_factor1;
+    p->drag_corr[1] = Correct_factor2;
+    p->drag_drag0[0] = Drag0_1;
+    p->drag_drag0[1] = Drag0_2;
+    p->drag_model = 1;
+}
+
 void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
     memset(p, 0, sizeof(*p));
     const double T = pfo_temperature(m, time);
@@ -156,9 +277,11 @@ void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
     p->diff_dt = m->dx * m->dx / maxD / p->dims * 0.2;
 
     p->df_model = 0;
+    p->drag_model = 0;
     p->avg_range = m->avg_carbon ? m->i_intf + 1 : 0; /* sparse.f90:186 */
     if (m->thermo_model == 1) {
         f90_thermo(T, p);
+        if (m->drag) f90_drag(m, T, p);
     } else {
         /* thermo_data.cpp:25-32: functor evaluation; linear_functor.h:11-13,
          * quadratic_functor.h:12-14.  Unset functors are zero. */
@@ -296,6 +419,8 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
     const double factor3 = PFO_PI / p->eta;
     double local_conc[4];
     for (int ii = 1; ii <= 3; ii++) local_conc[ii] = dfconc[3 * n + ii - 1]; /* carbon */
+    double drag[PFO_NSTENCIL + 1];
+    for (int ii = 0; ii <= PFO_NSTENCIL; ii++) drag[ii] = 0.;
     for (int ii = 1; ii <= num; ii++) {
         const int gi = sid[ii], phi_ = sph[ii];
         (void)gi;
@@ -311,7 +436,52 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
                  driving_force(p, phi_, phj, local_conc[phi_], local_conc[phj]);
             d *= M3(p->m, phi_, phj);
             del[ii] += d;
+            /* sparse.f90:287-292: Drag_ij = Factor3 sqrt(phi_i phi_j) for
+             * ferrite/austenite, times the mobility */
+            if (p->drag_model && phi_ + phj == 3) drag[ii] += M3(p->m, phi_, phj) * (factor3 * sqrt(sv1[ii] * sv1[jj]));
         }
+    }
+    /* sparse.f90:326-360: the Fortran model's solute drag.  Only in a cell
+     * with ferrite and austenite (Flag_coexist(2)) and without ferrite and
+     * cementite (Flag_coexist(1)) above the cutoff, only for the cell's own
+     * grains (Ii <= N_nonzero); positive rates of austenite and negative ones
+     * of ferrite are growth (DISSIPATION_ITERATION), the others shrinkage
+     * (_R); a rate of zero stays zero; with two entries the second rate is
+     * the negative of the first (sparse.f90:363-366). */
+    if (p->drag_model) {
+        const int co1 = phase[3 * n] > cutoff && phase[3 * n + 2] > cutoff;
+        const int co2 = phase[3 * n] > cutoff && phase[3 * n + 1] > cutoff;
+        int n_nonzero = 0;
+        for (int a = 0; a < PFO_NSLOT; a++)
+            if (phi1[6 * n + a] > cutoff) n_nonzero++;
+        for (int ii = 1; ii <= num; ii++) {
+            if (!co1 && co2 && ii <= n_nonzero) {
+                const double driv = del[ii];
+                const double norm = factor3 * sqrt(sv1[ii] * (1. - sv1[ii])); /* Normal_vec, sparse.f90:263-264 */
+                double lst = driv;                                            /* Lst_tmp(Ii) = Driv_matrix(Ii) */
+                if (driv > 0.) {
+                    if (sph[ii] == 2)
+                        lst = f90_dissipation(lst, driv, drag[ii], norm, 1, p);
+                    else if (sph[ii] == 1)
+                        lst = f90_dissipation(lst, driv, drag[ii], norm, 0, p);
+                } else if (driv < 0.) {
+                    if (sph[ii] == 1)
+                        lst = f90_dissipation(lst, -driv, drag[ii], norm, 1, p);
+                    else if (sph[ii] == 2)
+                        lst = f90_dissipation(lst, -driv, drag[ii], norm, 0, p);
+                    lst = -lst;
+                } else {
+                    lst = 0.;
+                }
+                del[ii] = lst;
+            }
+            if (num == 2) {
+                del[2] = -del[1];
+                break;
+            }
+        }
+    }
+    for (int ii = 1; ii <= num; ii++) {
         del[ii] *= p->pfm_dt;
         del[ii] += sv1[ii];
         if (del[ii] > 1.0) del[ii] = 1.0;

@@ -52,6 +52,8 @@ typedef struct {
     double mn_ratio[3];           /* Mn partition ratios r_p: c_p = r_p * c_ref (solute 2 only) */
     int thermo_model;             /* 1: the Fortran model's polynomial thermodynamics (sparse.f90:797-923) */
     int avg_carbon;               /* 1: interface-averaged concentrations in the driving force (sparse.f90:184-255) */
+    int drag;                     /* 1: Purdy-Brechet solute drag (sparse.f90:326-360, 538-671, 958-1041) */
+    double drag_binding, drag_vmax0, drag_qsd;
 } pfo_model;
 
 typedef struct {
@@ -68,6 +70,9 @@ typedef struct {
     int df_model;                 /* 1: driving force -ratio_ij*(max(c_i,c_j) - ref) (sparse.f90:512-515) */
     double df_ratio[9], df_ref;
     int avg_range;                /* > 0: half-width of the averaged neighbourhood (i_intf + 1) */
+    int drag_model;
+    double drag_vmax, drag_ex0, drag_de_heat, drag_de_cool, drag_u0;
+    double drag_corr[2], drag_drag0[2];
 } pfo_params;
 
 typedef struct {
@@ -111,6 +116,10 @@ int pfo_gpu_diffusion_solver(const double *D3, const double *k9, const double *c
 void pfo_fractions(const pfo_model *m, const int32_t *ids, const double *phi, const double *phase,
                    double *out4);
 int pfo_num_threads(void);
+/* Nonzero once a solute-drag iteration found no root (cleared by the caller). */
+extern int pfo_drag_failures;
+double pfo_exp(double x);
+double pfo_log(double x);
 void pfo_set_num_threads(int n);
 
 #ifdef __cplusplus

@@ -40,6 +40,8 @@ class OModel(ctypes.Structure):
         ("mn_ratio", _d3),
         ("thermo_model", ctypes.c_int),
         ("avg_carbon", ctypes.c_int),
+        ("drag", ctypes.c_int),
+        ("drag_binding", ctypes.c_double), ("drag_vmax0", ctypes.c_double), ("drag_qsd", ctypes.c_double),
     ]
 
 
@@ -57,6 +59,10 @@ class OParams(ctypes.Structure):
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
         ("avg_range", ctypes.c_int),
+        ("drag_model", ctypes.c_int),
+        ("drag_vmax", ctypes.c_double), ("drag_ex0", ctypes.c_double), ("drag_de_heat", ctypes.c_double),
+        ("drag_de_cool", ctypes.c_double), ("drag_u0", ctypes.c_double),
+        ("drag_corr", ctypes.c_double * 2), ("drag_drag0", ctypes.c_double * 2),
     ]
 
 
@@ -159,14 +165,20 @@ def parse_thermo(path: str, out: dict) -> None:
         out[k] = [0.0] * 9
     out["thermo_model"] = 0
     out["avg_carbon"] = 0
+    out["drag"] = 0
     if text.split()[:1] == ["F90_POLYNOMIAL"]:  # the Fortran model's built-in polynomials
         out["thermo_model"] = 1
         for line in text.splitlines()[1:]:
             words = line.split()
-            if words and not words[0].startswith("#"):
-                if words[0] != "AVERAGED_INTERFACE_CARBON":
-                    raise ValueError(f"thermo file: unknown keyword {words[0]}")
+            if not words or words[0].startswith("#"):
+                continue
+            if words[0] == "AVERAGED_INTERFACE_CARBON":
                 out["avg_carbon"] = 1
+            elif words[0] == "SOLUTE_DRAG":
+                out["drag"] = 1
+                out["drag_binding"], out["drag_vmax0"], out["drag_qsd"] = (float(w) for w in words[1:4])
+            else:
+                raise ValueError(f"thermo file: unknown keyword {words[0]}")
         return
     s = _Stream(text)
     s.ignore(3)
@@ -260,6 +272,9 @@ def model_from_dict(d: dict) -> OModel:
     m.nsol = d["nsol"]
     m.thermo_model = d.get("thermo_model", 0)
     m.avg_carbon = d.get("avg_carbon", 0)
+    m.drag = d.get("drag", 0)
+    if m.drag:
+        m.drag_binding, m.drag_vmax0, m.drag_qsd = d["drag_binding"], d["drag_vmax0"], d["drag_qsd"]
     for q in range(2):
         for p in range(3):
             m.D0[q][p], m.DQ[q][p] = d["D0"][q][p], d["DQ"][q][p]
@@ -307,6 +322,24 @@ def partition_all(m: OModel, p: OParams, phase, C, conc) -> None:
 def phase_sweep(m: OModel, p: OParams, ids1, phi1, ids2, phi2, phase, conc1, C) -> None:
     lib().pfo_phase_sweep(ctypes.byref(m), ctypes.byref(p), _ptr(ids1), _ptr(phi1), _ptr(ids2), _ptr(phi2),
                           _ptr(phase), _ptr(conc1), _ptr(C))
+
+
+def exp_log(x: np.ndarray):
+    """The shared pf_exp/pf_log of the drag solve, element-wise."""
+    L = lib()
+    L.pfo_exp.restype = L.pfo_log.restype = ctypes.c_double
+    L.pfo_exp.argtypes = L.pfo_log.argtypes = [ctypes.c_double]
+    x = np.asarray(x, dtype=np.float64).ravel()
+    return (np.array([L.pfo_exp(float(v)) for v in x]), np.array([L.pfo_log(float(v)) if v > 0 else np.nan for v in x]))
+
+
+def drag_failures(clear: bool = True) -> int:
+    """Whether a solute-drag iteration found no root since the last call."""
+    v = ctypes.c_int.in_dll(lib(), "pfo_drag_failures")
+    out = v.value
+    if clear:
+        v.value = 0
+    return out
 
 
 def avg_conc(m: OModel, p: OParams, phase, conc1) -> np.ndarray:

@@ -68,6 +68,8 @@ class PfModel(ctypes.Structure):
         ("eq_a", _d9), ("eq_b", _d9), ("eq_c", _d9),
         ("thermo_model", ctypes.c_int),
         ("avg_carbon", ctypes.c_int),
+        ("drag", ctypes.c_int),
+        ("drag_binding", ctypes.c_double), ("drag_vmax0", ctypes.c_double), ("drag_qsd", ctypes.c_double),
     ]
 
 
@@ -90,6 +92,10 @@ class PfStepParams(ctypes.Structure):
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
         ("avg_range", ctypes.c_int),
+        ("drag_model", ctypes.c_int),
+        ("drag_vmax", ctypes.c_double), ("drag_ex0", ctypes.c_double), ("drag_de_heat", ctypes.c_double),
+        ("drag_de_cool", ctypes.c_double), ("drag_u0", ctypes.c_double),
+        ("drag_corr", ctypes.c_double * 2), ("drag_drag0", ctypes.c_double * 2),
     ]
 
 

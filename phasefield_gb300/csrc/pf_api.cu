@@ -351,8 +351,8 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         return pf_fail(PF_ERR_ARG, "pf_create: bad model");
     if (precision == PF_PREC_FP32C && (long long)model->ix * model->iy * model->iz > 0xffffffffLL)
         return pf_fail(PF_ERR_RANGE, "pf_create: the compact FP32 path indexes cells with 32 bits");
-    if (precision == PF_PREC_FP32C && model->avg_carbon)
-        return pf_fail(PF_ERR_ARG, "pf_create: the interface-averaged carbon runs on the FP64 path only");
+    if (precision == PF_PREC_FP32C && (model->avg_carbon || model->drag))
+        return pf_fail(PF_ERR_ARG, "pf_create: the interface-averaged carbon and the solute drag run on the FP64 path only");
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
         cudaGetLastError();
@@ -711,6 +711,9 @@ extern "C" int pf_synchronize(pf_ctx *c) {
     PF_CUDA_OK(cudaStreamSynchronize(c->stream));
     if (pf_diffuse_take_timeout())
         return pf_fail(PF_ERR_TIMEOUT, "pf_synchronize: a bounded wait of the staged diffusion kernel ran out");
+    if (c->model.drag && pf_drag_take_failure())
+        return pf_fail(PF_ERR_RANGE, "pf_synchronize: a solute-drag velocity iteration found no root "
+                                     "(the Fortran model stops there)");
     return PF_OK;
 }
 
@@ -798,7 +801,8 @@ extern "C" int pf_batch_create(const pf_model *models, int ndom, pf_batch **out)
         const pf_model &m = models[d];
         if (m.iz != 1) return pf_fail(PF_ERR_ARG, "pf_batch_create: batched domains are 2D (iz == 1)");
         if (m.nsol != models[0].nsol) return pf_fail(PF_ERR_ARG, "pf_batch_create: all domains need the same solutes");
-        if (m.avg_carbon) return pf_fail(PF_ERR_ARG, "pf_batch_create: the interface-averaged carbon runs on the FP64 path only");
+        if (m.avg_carbon || m.drag)
+            return pf_fail(PF_ERR_ARG, "pf_batch_create: the interface-averaged carbon and the solute drag run on the FP64 path only");
         for (int t = 1; t < m.nT; t++)
             if (m.T_temp[t] != m.T_temp[0])
                 return pf_fail(PF_ERR_ARG, "pf_batch_create: each domain needs a constant temperature");

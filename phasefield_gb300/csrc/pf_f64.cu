@@ -11,7 +11,10 @@
 //   ids[6n+s] int32, phi[6n+s] f64, phase[3n+p] f64,
 //   conc[q*3N + 3n+p] f64, C[q*N + n] f64.
 #include "pf_dev.cuh"
+#include "pf_drag.h"
 #include "pf_kernels.h"
+
+__device__ int g_drag_fail;  // a solute-drag iteration found no root (the Fortran stops there)
 
 namespace {
 
@@ -239,9 +242,11 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
 
     const double factor1 = P.factor1, factor2 = P.factor2, factor3 = P.factor3;
     double del[PF_NSTENCIL];
+    double drag[PF_NSTENCIL];  // sum over ferrite/austenite partners of m_ij f3 sqrt(phi_i phi_j) (solute drag)
 #pragma unroll
     for (int ii = 0; ii < PF_NSTENCIL; ii++) {
         del[ii] = 0.;
+        drag[ii] = 0.;
         if (ii < num) {
             const int pi = sph[ii];
 #pragma unroll
@@ -261,9 +266,59 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                         d += factor3 * sqrt(s1[ii] * s1[jj]) * dfe;
                         d *= P.m[e];
                         del[ii] += d;
+                        if (P.drag_model && pi + pj == 3) drag[ii] += P.m[e] * (factor3 * sqrt(s1[ii] * s1[jj]));
                     }
                 }
             }
+        }
+    }
+    // The Fortran model's solute drag (sparse.f90:326-360): in a cell holding
+    // ferrite and austenite but not ferrite and cementite above the cutoff,
+    // each of the cell's own grains moves at the rate that balances its
+    // driving rate against the drag; a two-entry stencil keeps the second
+    // rate the negative of the first.
+    if (P.drag_model) {
+        const double f = phase[3 * n], a = phase[3 * n + 1], c = phase[3 * n + 2];
+        const bool co1 = f > cutoff && c > cutoff, co2 = f > cutoff && a > cutoff;
+        int nown = 0;
+#pragma unroll
+        for (int a6 = 0; a6 < 6; a6++) nown += own_v[a6] > cutoff ? 1 : 0;
+        int fail = 0;
+        for (int ii = 0; ii < num; ii++) {
+            if (!co1 && co2 && ii < nown) {
+                const double drv = del[ii];
+                const double norm = factor3 * sqrt(s1[ii] * (1. - s1[ii]));
+                double r = drv;
+                if (drv > 0.) {
+                    if (sph[ii] == 2)
+                        r = pf_drag_solve(drv, drag[ii], norm, 1, drv, P.drag_vmax, P.drag_ex0, P.drag_de_heat,
+                                          P.drag_u0, P.drag_corr[0], P.drag_drag0[0], P.T, &fail);
+                    else if (sph[ii] == 1)
+                        r = pf_drag_solve(drv, drag[ii], norm, 0, drv, P.drag_vmax, P.drag_ex0, P.drag_de_cool,
+                                          P.drag_u0, P.drag_corr[1], P.drag_drag0[1], P.T, &fail);
+                } else if (drv < 0.) {
+                    if (sph[ii] == 1)
+                        r = pf_drag_solve(-drv, drag[ii], norm, 1, drv, P.drag_vmax, P.drag_ex0, P.drag_de_heat,
+                                          P.drag_u0, P.drag_corr[0], P.drag_drag0[0], P.T, &fail);
+                    else if (sph[ii] == 2)
+                        r = pf_drag_solve(-drv, drag[ii], norm, 0, drv, P.drag_vmax, P.drag_ex0, P.drag_de_cool,
+                                          P.drag_u0, P.drag_corr[1], P.drag_drag0[1], P.T, &fail);
+                    r = -r;
+                } else {
+                    r = 0.;
+                }
+                del[ii] = r;
+            }
+            if (num == 2) {
+                del[1] = -del[0];
+                break;
+            }
+        }
+        if (fail) atomicExch(&g_drag_fail, 1);
+    }
+#pragma unroll
+    for (int ii = 0; ii < PF_NSTENCIL; ii++) {
+        if (ii < num) {
             del[ii] *= P.pfm_dt;
             del[ii] += s1[ii];
             if (del[ii] > 1.0) del[ii] = 1.0;
@@ -431,4 +486,17 @@ cudaError_t pf_launch_partition_f64(const pf_step_params &P, const double *phase
                                     double *conc, cudaStream_t s) {
     k_partition_f64<<<pf_blocks(P.N, 256), 256, 0, s>>>(P, phase, C, conc);
     return cudaGetLastError();
+}
+
+int pf_drag_take_failure() {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_drag_fail, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (v) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_drag_fail, &zero, sizeof(int));
+    }
+    return v;
 }

@@ -14,6 +14,8 @@
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
+
+#include "pf_drag.h"
 #endif
 #include "pf_host.h"
 #include "pf_init.h"
@@ -74,6 +76,8 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
     }
     m->thermo_model = 0;
     m->avg_carbon = 0;
+    m->drag = 0;
+    m->drag_binding = m->drag_vmax0 = m->drag_qsd = 0.;
     {
         std::string word;
         f >> word;
@@ -87,7 +91,11 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
                 std::string kw;
                 if (!(ls >> kw) || kw[0] == '#') continue;
                 if (kw == "AVERAGED_INTERFACE_CARBON") m->avg_carbon = 1;
-                else return pf_fail(PF_ERR_IO, "thermo file: unknown keyword " + kw);
+                else if (kw == "SOLUTE_DRAG") {  // binding energy, v_max0, Q_sd (pre_process.f90:150-151)
+                    if (!(ls >> m->drag_binding >> m->drag_vmax0 >> m->drag_qsd) || !(m->drag_vmax0 > 0.))
+                        return pf_fail(PF_ERR_IO, "thermo file: SOLUTE_DRAG needs binding energy, v_max0 > 0, Q_sd");
+                    m->drag = 1;
+                } else return pf_fail(PF_ERR_IO, "thermo file: unknown keyword " + kw);
             }
             return PF_OK;
         }
@@ -323,6 +331,53 @@ void pf_f90_thermo(double T, pf_step_params &p) {
     p.df_model = 1;
 }
 
+// PARAMETER_DRAG_PB (sparse.f90:958-1003) at temperature T, after
+// pf_f90_thermo: v_max, E0, the heating / cooling segregation parameters of
+// the three species (the bulk fractions Ux0 and the NPLE lines M_nple, N_nple
+// of the Fortran), and the correction factors that make the zero-velocity
+// drag equal the NPLE driving force |Ratio_k_para(2,1) (Ref_c_para(2,1) -
+// Ref_c_nple(2,1))| (heating; Ref_c_nple_r for cooling, sparse.f90:870-880,
+// zero below 1041.3 K where the Fortran leaves it at its initial value).
+void pf_f90_drag(const pf_model &m, double T, pf_step_params &p) {
+    const double x = T - 273.15;
+    p.drag_vmax = m.drag_vmax0 * pf_exp(-m.drag_qsd / (8.314 * T));
+    double M[3], Nn[3];
+    M[0] = std::max(1.E-10, 3.9793e-5 * x - 2.3163e-2);
+    M[1] = std::max(1.E-10, -2.928e-8 * (x * x) + 5.629e-5 * x - 2.35e-2);
+    M[2] = std::max(1.E-10, 2.253e-8 * (x * x) - 4.255e-5 * x + 2.351e-2);
+    Nn[0] = std::max(1.E-10, -3.818e-9 * (x * x * x) + 9.055e-6 * (x * x) - 7.408e-3 * x + 2.118);
+    Nn[1] = std::max(1.E-10, -7.1227e-10 * (x * x * x) + 1.6307e-6 * (x * x) - 1.2584e-3 * x + 3.3166e-1);
+    Nn[2] = 3.E-3;
+    const double U[3] = {1.887e-2, 3.65e-3, 3.12e-3};
+    double deh[3], dec[3];
+    for (int i = 0; i < 3; i++) {
+        deh[i] = -0.5 * pf_log(M[i] * (1. - U[i]) / (U[i] * (1. - M[i])));
+        dec[i] = -0.5 * pf_log(Nn[i] * (1. - U[i]) / (U[i] * (1. - Nn[i])));
+    }
+    p.drag_ex0 = m.drag_binding / (8.314 * T);
+    auto poly4 = [](double y, double a, double b, double c, double d) {
+        return a * y + b * y * y + c * y * y * y + d * y * y * y * y;
+    };
+    const double nple21 = T < 1110.64 ? poly4(T - 1110.64, -3.3441e-3, 1.0406e-5, -5.6345e-8, 0.0)
+                                      : poly4(T - 1110.64, -3.23154e-3, 0., 0., 0.);
+    const double nple_r21 = T < 1041.3 ? 0. : -2.39e-3 * (T - 1041.3);
+    const double ratio21 = p.df_ratio[e3(2, 1)], ref21 = p.eq[e3(2, 1)];
+    const double driv_f[2] = {std::abs(ratio21 * (ref21 - nple21)), std::abs(ratio21 * (ref21 - nple_r21))};
+    const double vmax = p.drag_vmax;
+    double d0h = pf_solute_drag_pb(0., p.drag_ex0, deh[0], U[0], vmax, T) + pf_solute_drag_pb(0., 0., deh[1], U[1], vmax, T) +
+                 pf_solute_drag_pb(0., 0., deh[2], U[2], vmax, T);
+    double d0c = pf_solute_drag_pb(0., p.drag_ex0, dec[0], U[0], vmax, T) + pf_solute_drag_pb(0., 0., dec[1], U[1], vmax, T) +
+                 pf_solute_drag_pb(0., 0., dec[2], U[2], vmax, T);
+    p.drag_corr[0] = driv_f[0] / d0h;
+    p.drag_corr[1] = driv_f[1] / d0c;
+    p.drag_drag0[0] = pf_solute_drag_pb(0., p.drag_ex0, deh[0], U[0], vmax, T) * p.drag_corr[0];
+    p.drag_drag0[1] = pf_solute_drag_pb(0., p.drag_ex0, dec[0], U[0], vmax, T) * p.drag_corr[1];
+    p.drag_de_heat = deh[0];
+    p.drag_de_cool = dec[0];
+    p.drag_u0 = U[0];
+    p.drag_model = 1;
+}
+
 void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
     std::memset(&p, 0, sizeof(p));
     p.ix = m.ix; p.iy = m.iy; p.iz = m.iz;
@@ -357,6 +412,7 @@ void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
     p.avg_range = m.avg_carbon ? m.i_intf + 1 : 0;  // sparse.f90:186
     if (m.thermo_model == 1) {
         pf_f90_thermo(T, p);
+        if (m.drag) pf_f90_drag(m, T, p);
     } else {
         // thermo_data.cpp:25-32 with linear_functor.h / quadratic_functor.h
         for (int j = 1; j <= 3; j++)

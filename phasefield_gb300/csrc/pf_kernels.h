@@ -9,6 +9,9 @@
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
                                 double *phi2, double *phase, double *conc1, const double *C, double *avg,
                                 cudaStream_t s);
+// 1 if a solute-drag velocity iteration of the FP64 sweep found no root since
+// the last call (then cleared).
+int pf_drag_take_failure();
 cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
                                   const double *conc1, double *conc2, double *C, cudaStream_t s);
 cudaError_t pf_launch_partition_f64(const pf_step_params &P, const double *phase, const double *C,

@@ -75,12 +75,20 @@ THERMO_F90_TEXT = """F90_POLYNOMIAL
 """
 
 
+# Solute-drag parameters of the Fortran model's sample input
+# (Fortran_openmp_phase_field/PFM/example/log_file.txt, last block): binding
+# energy 10000 J/mol, v_m0 1e11 um/s, Q_sd 247650 J/mol.
+F90_DRAG_LINE = "SOLUTE_DRAG 10000. 1.0e11 247650.\n"
+
+
 def write_thermo(path: str, model: str = "linear") -> str:
     """model: "linear" (the reference's sample lines), "f90" (the Fortran
-    model's thermodynamics) or "f90avg" (that, plus the interface-averaged
-    carbon of sparse.f90:184-255)."""
+    model's thermodynamics), "f90avg" (that, plus the interface-averaged
+    carbon of sparse.f90:184-255) or "f90drag" (that, plus the solute drag of
+    sparse.f90:326-360 with the Fortran sample's parameters)."""
     text = {"linear": THERMO_TEXT, "f90": THERMO_F90_TEXT,
-            "f90avg": THERMO_F90_TEXT + "AVERAGED_INTERFACE_CARBON\n"}[model]
+            "f90avg": THERMO_F90_TEXT + "AVERAGED_INTERFACE_CARBON\n",
+            "f90drag": THERMO_F90_TEXT + F90_DRAG_LINE}[model]
     with open(path, "w") as f:
         f.write(text)
     return path

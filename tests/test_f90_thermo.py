@@ -201,3 +201,113 @@ def test_averaged_carbon_keyword_and_precision_checks(tmp_path):
     m = pf.read_model(cfg)
     h = pf.ctypes.c_void_p()
     assert pf.lib().pf_create(pf.ctypes.byref(m), pf.PF_PREC_FP32C, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
+
+
+def _drag_case(tmp_path, grid=(48, 40, 1), T=1023.0, model="f90drag"):
+    W.write_thermo(str(tmp_path / "thermo_drag.txt"), model)
+    cfg = W.write_config(str(tmp_path / "drag.txt"), grid=grid, T=T, thermo_file="thermo_drag.txt",
+                         directory=str(tmp_path / "out"))
+    return pf.read_model(cfg), po.load_model(cfg)
+
+
+def _sd_literal(V0, E0, De, U0, V_max, T):
+    """SOLUTE_DRAG_PB (sparse.f90:1005-1037) in Python floats."""
+    import math
+    V = V0 / V_max
+    A = (De - E0) + V
+    B = (De + E0) + V
+    D0 = 1. - U0
+    Vu0 = V * U0
+    D1_d0 = (A - Vu0) / (A * D0 + (A - V) * U0 * math.exp(-(A - Vu0)))
+    D1 = D0 * D1_d0
+    U1 = 1. - D1
+    D2_d1 = (B - Vu0) / (B * D1 + (B * U1 - Vu0) * math.exp(-(B - Vu0)))
+    return (2. * De * U0 - ((A - V) / A * (Vu0 + math.log(D1_d0)) + (B - V) / B * (Vu0 + math.log(D2_d1)))) * 8.314 * T / 7.2e12
+
+
+@pytest.mark.parametrize("T", [1000.0, 1023.0, 1050.0, 1120.0])
+def test_drag_parameters_product_oracle_and_fortran_literal(tmp_path, T):
+    """PARAMETER_DRAG_PB: the product's values equal the oracle's bit for bit;
+    both agree with a literal Python restatement (Python's exp/log) to 1e-13."""
+    import math
+    m, om = _drag_case(tmp_path, T=T)
+    assert m.drag == 1 and om.drag == 1 and m.drag_vmax0 == 1.0e11
+    p, q = pf.params_at(m, 0.0), po.params_at(om, 0.0)
+    assert p.drag_model == 1 and q.drag_model == 1
+    for name in ("drag_vmax", "drag_ex0", "drag_de_heat", "drag_de_cool", "drag_u0"):
+        assert getattr(p, name) == getattr(q, name), name
+    assert list(p.drag_corr) == list(q.drag_corr) and list(p.drag_drag0) == list(q.drag_drag0)
+    # sparse.f90:958-1003 literally
+    x = T - 273.15
+    vmax = 1.0e11 * math.exp(-247650. / (8.314 * T))
+    Mn = [max(1e-10, 3.9793e-5 * x - 2.3163e-2), max(1e-10, -2.928e-8 * x ** 2 + 5.629e-5 * x - 2.35e-2),
+          max(1e-10, 2.253e-8 * x ** 2 - 4.255e-5 * x + 2.351e-2)]
+    Nn = [max(1e-10, -3.818e-9 * x ** 3 + 9.055e-6 * x ** 2 - 7.408e-3 * x + 2.118),
+          max(1e-10, -7.1227e-10 * x ** 3 + 1.6307e-6 * x ** 2 - 1.2584e-3 * x + 3.3166e-1), 3e-3]
+    U = [1.887e-2, 3.65e-3, 3.12e-3]
+    deh = [-0.5 * math.log(Mn[i] * (1 - U[i]) / (U[i] * (1 - Mn[i]))) for i in range(3)]
+    dec = [-0.5 * math.log(Nn[i] * (1 - U[i]) / (U[i] * (1 - Nn[i]))) for i in range(3)]
+    ex0 = 10000. / (8.314 * T)
+    y = T - 1110.64
+    nple = (-3.3441e-3 * y + 1.0406e-5 * y * y - 5.6345e-8 * y ** 3) if T < 1110.64 else -3.23154e-3 * y
+    nple_r = 0.0 if T < 1041.3 else -2.39e-3 * (T - 1041.3)
+    r21, ref21 = p.df_ratio[1], p.eq[1]  # (2,1) at (2-1)+3*(1-1)
+    drivf = [abs(r21 * (ref21 - nple)), abs(r21 * (ref21 - nple_r))]
+    d0 = [sum(_sd_literal(0., ex0 if i == 0 else 0., de[i], U[i], vmax, T) for i in range(3)) for de in (deh, dec)]
+    corr = [drivf[0] / d0[0], drivf[1] / d0[1]]
+    drag0 = [_sd_literal(0., ex0, deh[0], U[0], vmax, T) * corr[0], _sd_literal(0., ex0, dec[0], U[0], vmax, T) * corr[1]]
+    np.testing.assert_allclose([p.drag_vmax, p.drag_ex0, p.drag_de_heat, p.drag_de_cool],
+                               [vmax, ex0, deh[0], dec[0]], rtol=1e-13)
+    np.testing.assert_allclose(list(p.drag_corr) + list(p.drag_drag0), corr + drag0, rtol=1e-12)
+
+
+def test_drag_changes_the_oracle_step(tmp_path):
+    """With the solute drag the oracle advances the ferrite/austenite
+    interfaces differently, finds a velocity root wherever it solves, and
+    keeps carbon."""
+    grid = (48, 40, 1)
+    _, om = _drag_case(tmp_path, grid=grid)
+    (tmp_path / "plain").mkdir()
+    _, om2 = _drag_case(tmp_path / "plain", grid=grid, model="f90")
+    spec = W.WORKLOADS["2d256"].spec()
+    spec.n_grains, spec.n_nuclei = 4, 5
+    st = po.init_state(om, spec, 0.0)
+    st2 = {k: v.copy() for k, v in st.items()}
+    N = grid[0] * grid[1]
+    tot0 = st["C"][:N].sum()
+    po.drag_failures()
+    po.run(om, st, 0.0, 10)
+    po.run(om2, st2, 0.0, 10)
+    assert po.drag_failures() == 0
+    assert not np.array_equal(st["phi"], st2["phi"])
+    assert abs(st["C"][:N].sum() - tot0) / tot0 < 1e-12
+
+
+def test_shared_exp_log_against_c_library():
+    """pf_exp/pf_log (the drag solve's own exp and log) stay within 4 ulp of
+    the C library over the arguments the drag model meets and well beyond."""
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.uniform(-700, 700, 4000), rng.uniform(-2, 2, 4000), [0.0, -0.0, 1e-300, -1e-300]])
+    e, _ = po.exp_log(x)
+    ref = np.exp(x)
+    assert np.all(np.abs(e - ref) <= 4 * np.spacing(ref))
+    y = np.concatenate([10.0 ** rng.uniform(-300, 300, 4000), rng.uniform(0.5, 2.0, 4000), [1.0, 2.0, 0.5]])
+    _, lg = po.exp_log(y)
+    ref = np.log(y)
+    assert np.all(np.abs(lg - ref) <= 4 * np.spacing(np.abs(ref)) + 1e-300)
+    assert lg[-3] == 0.0
+
+
+def test_solute_drag_keyword_and_precision(tmp_path):
+    """`SOLUTE_DRAG b v q` sets the model's drag fields; a line with missing
+    values is an input error; compact FP32 contexts refuse the option."""
+    m, om = _drag_case(tmp_path)
+    assert (m.drag_binding, m.drag_vmax0, m.drag_qsd) == (10000.0, 1.0e11, 247650.0)
+    assert (om.drag_binding, om.drag_vmax0, om.drag_qsd) == (10000.0, 1.0e11, 247650.0)
+    (tmp_path / "bad.txt").write_text("F90_POLYNOMIAL\nSOLUTE_DRAG 10000. 1.0e11\n")
+    cfg = W.write_config(str(tmp_path / "c_bad.txt"), grid=(8, 8, 1), thermo_file="bad.txt",
+                         directory=str(tmp_path / "out"))
+    with pytest.raises(pf.PfError):
+        pf.read_model(cfg)
+    h = pf.ctypes.c_void_p()
+    assert pf.lib().pf_create(pf.ctypes.byref(m), pf.PF_PREC_FP32C, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
