@@ -129,6 +129,16 @@ typedef struct {
      * F90_POLYNOMIAL in the thermo file (J/mol, um/s, J/mol). */
     int drag;
     double drag_binding, drag_vmax0, drag_qsd;
+    /* 1: the Fortran model's coherent-grain mobility (sparse.f90:298-315;
+     * FP64 path only): a ferrite/austenite pair whose austenite grain nucleated
+     * coherent with that ferrite grain (pf_set_coherent_grains) moves at 0.02
+     * of its mobility in a cell with one own ferrite grain whose interface
+     * neighbourhood holds bulk ferrite and no recrystallisation front.
+     * Selected by "COHERENT_MOBILITY npp0" after F90_POLYNOMIAL in the thermo
+     * file; ferrite ids <= npp0 are the initial (deformed) grains, larger ones
+     * recrystallised (0: a single class, no recrystallisation fronts). */
+    int coherent;
+    int coh_npp0;
 } pf_model;
 
 /* Per-step parameters evaluated on the host (Update_parameter,
@@ -152,9 +162,12 @@ typedef struct {
      * = -df_ratio_ij * (max(c_i, c_j) - df_ref) */
     int df_model;
     double df_ratio[9], df_ref;
-    /* > 0: half-width (i_intf + 1 cells) of the neighbourhood averaged for
-     * the driving force's phase concentrations; 0: the cell's own */
+    /* > 0: half-width (i_intf + 1 cells) of the interface neighbourhood
+     * scanned before the sweep (averaged carbon, coherent-mobility flags);
+     * avg_conc = 1: the driving force reads the averaged phase
+     * concentrations, 0: the cell's own */
     int avg_range;
+    int avg_conc;
     /* Solute drag at the step's temperature (PARAMETER_DRAG_PB,
      * sparse.f90:958-1003): v_max, E0 = binding/RT, the Mn segregation
      * parameters of heating / cooling and the bulk fraction of the first
@@ -162,6 +175,10 @@ typedef struct {
     int drag_model;
     double drag_vmax, drag_ex0, drag_de_heat, drag_de_cool, drag_u0;
     double drag_corr[2], drag_drag0[2];
+    /* Coherent-grain mobility (pf_model.coherent) and the last id of the
+     * initial ferrite class */
+    int coh_model;
+    int coh_npp0;
 } pf_step_params;
 
 /* Seeded synthetic microstructure (replaces the reference's unseeded
@@ -322,6 +339,19 @@ int pf_write_vti(const char *path, int ix, int iy, int iz, double dx, const int3
  * values agree to a few ulp (the device's tanh).  PF_ERR_RANGE if more than
  * 256 nuclei or particles lie near one cell. */
 int pf_init_device(pf_ctx *ctx, const pf_init_spec *spec, double time);
+
+/* Coherent partners of the austenite grains (Fortran model's Coherent_grain,
+ * sparse.f90:298-315, set at nucleation by module_nucleation.f90:357-367):
+ * partners[2*n + k], k = 0, 1, is a ferrite grain id coherent with austenite
+ * grain 200001 + n, or 0; n_austenite <= 100000 entries (later austenite ids
+ * have none).  Copied to the device; replaces any earlier table.  Used by a
+ * model with coherent = 1 (PF_ERR_ARG otherwise). */
+int pf_set_coherent_grains(pf_ctx *ctx, const int32_t *partners, int n_austenite);
+/* The table of the seeded state of 'spec', by the Fortran's rule for
+ * nucleation in a grain boundary (module_nucleation.f90:357-367): at the cell
+ * of nucleus n, before any nucleus is laid, Or_num = min(2, number of ferrite
+ * grains - 1) partners, the largest ferrite ids there.  partners[2*n_nuclei]. */
+int pf_init_coherent(const pf_model *model, const pf_init_spec *spec, int32_t *partners);
 
 /* Microstructure files in appended raw binary VTK image data, written from
  * the device state while stepping continues (the MPI variant's piece files and

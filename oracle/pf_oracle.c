@@ -278,7 +278,10 @@ void pfo_params_at(const pfo_model *m, double time, pfo_params *p) {
 
     p->df_model = 0;
     p->drag_model = 0;
-    p->avg_range = m->avg_carbon ? m->i_intf + 1 : 0; /* sparse.f90:186 */
+    p->avg_range = (m->avg_carbon || m->coherent) ? m->i_intf + 1 : 0; /* sparse.f90:186 */
+    p->avg_conc = m->avg_carbon;
+    p->coh_model = m->coherent;
+    p->coh_npp0 = m->coh_npp0;
     if (m->thermo_model == 1) {
         f90_thermo(T, p);
         if (m->drag) f90_drag(m, T, p);
@@ -352,9 +355,20 @@ static inline double driving_force(const pfo_params *p, int phii, int phjj, doub
 }
 
 /* solver.cpp:147-304 (Phase_field_solver) for cell (i,j,k), 0-based. */
+/* Coherent_grain (pre_process.f90:238, module_nucleation.f90:357-367):
+ * two ferrite ids per austenite grain; Any(Coherent_grain(aus,:) == other) */
+static int32_t *pfo_coh = NULL;
+static int pfo_n_coh = 0;
+static int coherent_with(int aus, int other) {
+    const int k = aus - 200001;
+    if (k < 0 || k >= pfo_n_coh || other == 0) return 0;
+    return pfo_coh[2 * k] == other || pfo_coh[2 * k + 1] == other;
+}
+
 static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, int k,
                        const int32_t *ids1, const double *phi1, int32_t *ids2, double *phi2,
-                       double *phase, double *conc1, const double *C, const double *dfconc) {
+                       double *phase, double *conc1, const double *C, const double *dfconc,
+                       const unsigned char *flags) {
     const int ix = m->ix, iy = m->iy, iz = m->iz;
     const long N = (long)ix * iy * iz;
     const long n = i + (long)ix * (j + (long)iy * k);
@@ -421,9 +435,19 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
     for (int ii = 1; ii <= 3; ii++) local_conc[ii] = dfconc[3 * n + ii - 1]; /* carbon */
     double drag[PFO_NSTENCIL + 1];
     for (int ii = 0; ii <= PFO_NSTENCIL; ii++) drag[ii] = 0.;
+    /* sparse.f90:300-306: Count(Phase_index(Ind_ph1(1:N_nonzero))==1) == 1,
+     * .Not. Rex_intf, Has_ferrite */
+    int coh_cell = 0;
+    if (p->coh_model && flags) {
+        int n_nonzero = 0, n_ferrite = 0;
+        for (int a = 0; a < PFO_NSLOT; a++)
+            if (phi1[6 * n + a] > cutoff) n_nonzero++;
+        for (int a = 0; a < n_nonzero; a++)
+            if (pfo_phase_of_grain(ids1[6 * n + a]) == 1) n_ferrite++;
+        coh_cell = (flags[n] & 1) && !(flags[n] & 2) && n_ferrite == 1;
+    }
     for (int ii = 1; ii <= num; ii++) {
         const int gi = sid[ii], phi_ = sph[ii];
-        (void)gi;
         for (int jj = 1; jj <= num; jj++) {
             if (ii == jj) continue;
             const int phj = sph[jj];
@@ -434,11 +458,20 @@ static void phase_cell(const pfo_model *m, const pfo_params *p, int i, int j, in
             d *= M3(m->sigma, phi_, phj);
             d += factor3 * sqrt(sv1[ii] * sv1[jj]) *
                  driving_force(p, phi_, phj, local_conc[phi_], local_conc[phj]);
-            d *= M3(p->m, phi_, phj);
+            /* sparse.f90:298-315: a pair whose austenite grain is coherent
+             * with the other grain moves at 0.02 of the mobility */
+            const int coherent = coh_cell && ((phi_ == 2 && coherent_with(gi, sid[jj])) ||
+                                              (phj == 2 && coherent_with(sid[jj], gi)));
+            if (coherent) d = 0.02 * M3(p->m, phi_, phj) * d;
+            else d *= M3(p->m, phi_, phj);
             del[ii] += d;
             /* sparse.f90:287-292: Drag_ij = Factor3 sqrt(phi_i phi_j) for
              * ferrite/austenite, times the mobility */
-            if (p->drag_model && phi_ + phj == 3) drag[ii] += M3(p->m, phi_, phj) * (factor3 * sqrt(sv1[ii] * sv1[jj]));
+            if (p->drag_model && phi_ + phj == 3) {
+                const double drag_ij = factor3 * sqrt(sv1[ii] * sv1[jj]);
+                if (coherent) drag[ii] += 0.02 * M3(p->m, phi_, phj) * drag_ij;
+                else drag[ii] += M3(p->m, phi_, phj) * drag_ij;
+            }
         }
     }
     /* sparse.f90:326-360: the Fortran model's solute drag.  Only in a cell
@@ -532,8 +565,8 @@ static inline int f90_ngb(int c, int len, int n) {
  * cell (sparse.f90:141-146 and 184-255), from the phase fractions and phase
  * concentrations of the start of the sweep (the Fortran loop reads values
  * its own sweep may already have updated; here none are). */
-void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, const double *conc1,
-                  double *avg) {
+void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phase,
+                  const double *conc1, double *avg, unsigned char *flags) {
     const int ix = m->ix, iy = m->iy, iz = m->iz;
     const double cutoff = m->cutoff;
     const int R = p->avg_range;
@@ -544,6 +577,7 @@ void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, 
             for (int i = 0; i < ix; i++) {
                 const long n = i + (long)ix * (j + (long)iy * k);
                 double out[3] = {conc1[3 * n], conc1[3 * n + 1], conc1[3 * n + 2]};
+                int has_ferrite = 0, rex_intf = 0; /* sparse.f90:137-139 */
                 if (phase[3 * n] > cutoff && phase[3 * n + 1] > cutoff) { /* Flag_coexist(2) */
                     double G[3];
                     G[0] = PH1(f90_ngb(i, ix, 1), j, k) - PH1(f90_ngb(i, ix, -1), j, k);
@@ -568,7 +602,17 @@ void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, 
                                 if (distance > g2 * 1.0) continue;
                                 const long q = x + (long)ix * (y + (long)iy * z);
                                 const double p1 = phase[3 * q], p2 = phase[3 * q + 1];
+                                if (p1 > 1. - cutoff) has_ferrite = 1; /* sparse.f90:214-215 */
                                 if (p1 < cutoff || p2 < cutoff) continue;
+                                { /* sparse.f90:218-222: a deformed and a recrystallised ferrite grain */
+                                    int lo = 0, hi = 0;
+                                    for (int a = 0; a < PFO_NSLOT; a++) {
+                                        const int g = ids1[6 * q + a];
+                                        if (pfo_phase_of_grain(g) == 1 && g <= p->coh_npp0) lo = 1;
+                                        if (pfo_phase_of_grain(g) == 1 && g > p->coh_npp0) hi = 1;
+                                    }
+                                    rex_intf = rex_intf || (lo && hi);
+                                }
                                 const double h[3] = {PH1(f90_ngb(x, ix, 1), y, z) - PH1(f90_ngb(x, ix, -1), y, z),
                                                      PH1(x, f90_ngb(y, iy, 1), z) - PH1(x, f90_ngb(y, iy, -1), z),
                                                      PH1(x, y, f90_ngb(z, iz, 1)) - PH1(x, y, f90_ngb(z, iz, -1))};
@@ -585,25 +629,41 @@ void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, 
                         for (int d = 0; d < 3; d++) out[d] = sum[d] / num;
                 }
                 for (int d = 0; d < 3; d++) avg[3 * n + d] = out[d];
+                if (flags) flags[n] = (unsigned char)(has_ferrite | (rex_intf << 1));
             }
 #undef PH1
+}
+
+void pfo_set_coherent(const int32_t *partners, int n_austenite) {
+    free(pfo_coh);
+    pfo_coh = NULL;
+    pfo_n_coh = 0;
+    if (n_austenite > 0 && partners) {
+        pfo_coh = (int32_t *)malloc(2 * (size_t)n_austenite * sizeof(int32_t));
+        memcpy(pfo_coh, partners, 2 * (size_t)n_austenite * sizeof(int32_t));
+        pfo_n_coh = n_austenite;
+    }
 }
 
 void pfo_phase_sweep(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phi1,
                      int32_t *ids2, double *phi2, double *phase, double *conc1, const double *C) {
     double *avg = NULL;
+    unsigned char *flags = NULL;
     if (p->avg_range > 0) {
         const long N = (long)m->ix * m->iy * m->iz;
         avg = (double *)malloc(3 * N * sizeof(double));
-        pfo_avg_conc(m, p, phase, conc1, avg);
+        if (p->coh_model) flags = (unsigned char *)malloc(N);
+        pfo_avg_conc(m, p, ids1, phase, conc1, avg, flags);
     }
     /* phase_field.cpp:252-257 */
 #pragma omp parallel for schedule(guided, 1) collapse(2)
     for (int k = 0; k < m->iz; k++)
         for (int j = 0; j < m->iy; j++)
             for (int i = 0; i < m->ix; i++)
-                phase_cell(m, p, i, j, k, ids1, phi1, ids2, phi2, phase, conc1, C, avg ? avg : conc1);
+                phase_cell(m, p, i, j, k, ids1, phi1, ids2, phi2, phase, conc1, C,
+                           (avg && p->avg_conc) ? avg : conc1, flags);
     free(avg);
+    free(flags);
 }
 
 /* solver.cpp:343-372 (Diffusion_solver) for every solute */

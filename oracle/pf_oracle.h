@@ -54,6 +54,8 @@ typedef struct {
     int avg_carbon;               /* 1: interface-averaged concentrations in the driving force (sparse.f90:184-255) */
     int drag;                     /* 1: Purdy-Brechet solute drag (sparse.f90:326-360, 538-671, 958-1041) */
     double drag_binding, drag_vmax0, drag_qsd;
+    int coherent;                 /* 1: coherent-grain mobility (sparse.f90:298-315) */
+    int coh_npp0;                 /* last id of the initial ferrite class (Npp0) */
 } pfo_model;
 
 typedef struct {
@@ -69,10 +71,12 @@ typedef struct {
     double eta;
     int df_model;                 /* 1: driving force -ratio_ij*(max(c_i,c_j) - ref) (sparse.f90:512-515) */
     double df_ratio[9], df_ref;
-    int avg_range;                /* > 0: half-width of the averaged neighbourhood (i_intf + 1) */
+    int avg_range;                /* > 0: half-width of the scanned neighbourhood (i_intf + 1) */
+    int avg_conc;                 /* 1: the driving force reads the averaged concentrations */
     int drag_model;
     double drag_vmax, drag_ex0, drag_de_heat, drag_de_cool, drag_u0;
     double drag_corr[2], drag_drag0[2];
+    int coh_model, coh_npp0;
 } pfo_params;
 
 typedef struct {
@@ -97,9 +101,12 @@ void pfo_partition_all(const pfo_model *m, const pfo_params *p, const double *ph
 /* solver.cpp:147-304 over all cells (phase_field.cpp:252-257) */
 void pfo_phase_sweep(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phi1,
                      int32_t *ids2, double *phi2, double *phase, double *conc1, const double *C);
-/* sparse.f90:184-255: interface-averaged phase concentrations of every cell */
-void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const double *phase, const double *conc1,
-                  double *avg);
+/* sparse.f90:184-255: interface-averaged phase concentrations of every cell;
+ * flags (may be NULL): bit 0 Has_ferrite, bit 1 Rex_intf of the same scan */
+void pfo_avg_conc(const pfo_model *m, const pfo_params *p, const int32_t *ids1, const double *phase,
+                  const double *conc1, double *avg, unsigned char *flags);
+/* Coherent_grain: partners[2n + k] of austenite grain 200001 + n (copied) */
+void pfo_set_coherent(const int32_t *partners, int n_austenite);
 /* solver.cpp:343-372 over all cells (phase_field.cpp:274-280) */
 void pfo_diffusion_substep(const pfo_model *m, const pfo_params *p, double dt_sub, const double *phase,
                            const double *conc1, double *conc2, double *C);

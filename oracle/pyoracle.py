@@ -42,6 +42,7 @@ class OModel(ctypes.Structure):
         ("avg_carbon", ctypes.c_int),
         ("drag", ctypes.c_int),
         ("drag_binding", ctypes.c_double), ("drag_vmax0", ctypes.c_double), ("drag_qsd", ctypes.c_double),
+        ("coherent", ctypes.c_int), ("coh_npp0", ctypes.c_int),
     ]
 
 
@@ -58,11 +59,12 @@ class OParams(ctypes.Structure):
         ("dims", ctypes.c_double), ("eta", ctypes.c_double),
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
-        ("avg_range", ctypes.c_int),
+        ("avg_range", ctypes.c_int), ("avg_conc", ctypes.c_int),
         ("drag_model", ctypes.c_int),
         ("drag_vmax", ctypes.c_double), ("drag_ex0", ctypes.c_double), ("drag_de_heat", ctypes.c_double),
         ("drag_de_cool", ctypes.c_double), ("drag_u0", ctypes.c_double),
         ("drag_corr", ctypes.c_double * 2), ("drag_drag0", ctypes.c_double * 2),
+        ("coh_model", ctypes.c_int), ("coh_npp0", ctypes.c_int),
     ]
 
 
@@ -96,7 +98,9 @@ def lib() -> ctypes.CDLL:
         L.pfo_params_at.restype = None
         L.pfo_partition_all.argtypes = [M, PP, _P, _P, _P]
         L.pfo_phase_sweep.argtypes = [M, PP, _P, _P, _P, _P, _P, _P, _P]
-        L.pfo_avg_conc.argtypes = [M, PP, _P, _P, _P]
+        L.pfo_avg_conc.argtypes = [M, PP, _P, _P, _P, _P, _P]
+        L.pfo_set_coherent.argtypes = [_P, ctypes.c_int]
+        L.pfo_set_coherent.restype = None
         L.pfo_diffusion_substep.argtypes = [M, PP, _D, _P, _P, _P, _P]
         L.pfo_run.argtypes = [M, ctypes.POINTER(OState), ctypes.POINTER(ctypes.c_double), ctypes.c_int]
         L.pfo_gpu_diffusion_solver.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -166,6 +170,7 @@ def parse_thermo(path: str, out: dict) -> None:
     out["thermo_model"] = 0
     out["avg_carbon"] = 0
     out["drag"] = 0
+    out["coherent"] = 0
     if text.split()[:1] == ["F90_POLYNOMIAL"]:  # the Fortran model's built-in polynomials
         out["thermo_model"] = 1
         for line in text.splitlines()[1:]:
@@ -177,6 +182,9 @@ def parse_thermo(path: str, out: dict) -> None:
             elif words[0] == "SOLUTE_DRAG":
                 out["drag"] = 1
                 out["drag_binding"], out["drag_vmax0"], out["drag_qsd"] = (float(w) for w in words[1:4])
+            elif words[0] == "COHERENT_MOBILITY":
+                out["coherent"] = 1
+                out["coh_npp0"] = int(words[1])
             else:
                 raise ValueError(f"thermo file: unknown keyword {words[0]}")
         return
@@ -275,6 +283,8 @@ def model_from_dict(d: dict) -> OModel:
     m.drag = d.get("drag", 0)
     if m.drag:
         m.drag_binding, m.drag_vmax0, m.drag_qsd = d["drag_binding"], d["drag_vmax0"], d["drag_qsd"]
+    m.coherent = d.get("coherent", 0)
+    m.coh_npp0 = d.get("coh_npp0", 0)
     for q in range(2):
         for p in range(3):
             m.D0[q][p], m.DQ[q][p] = d["D0"][q][p], d["DQ"][q][p]
@@ -342,11 +352,26 @@ def drag_failures(clear: bool = True) -> int:
     return out
 
 
-def avg_conc(m: OModel, p: OParams, phase, conc1) -> np.ndarray:
-    """The interface-averaged phase concentrations of every cell (sparse.f90:184-255)."""
-    out = np.zeros_like(conc1[: 3 * m.ix * m.iy * m.iz])
-    lib().pfo_avg_conc(ctypes.byref(m), ctypes.byref(p), _ptr(phase), _ptr(conc1), _ptr(out))
-    return out
+def avg_conc(m: OModel, p: OParams, phase, conc1, ids=None, with_flags: bool = False):
+    """The interface-averaged phase concentrations of every cell (sparse.f90:184-255);
+    with_flags (needs ids): also the scan's Has_ferrite (bit 0) / Rex_intf (bit 1) bytes."""
+    N = m.ix * m.iy * m.iz
+    out = np.zeros_like(conc1[: 3 * N])
+    flags = np.zeros(N, np.uint8) if with_flags else None
+    ids = np.zeros(6 * N, np.int32) if ids is None else ids
+    lib().pfo_avg_conc(ctypes.byref(m), ctypes.byref(p), _ptr(ids), _ptr(phase), _ptr(conc1), _ptr(out),
+                       _ptr(flags))
+    return (out, flags) if with_flags else out
+
+
+def set_coherent(partners) -> None:
+    """Coherent_grain of the oracle: partners[n] = the two ferrite ids coherent
+    with austenite grain 200001 + n (None clears)."""
+    if partners is None:
+        lib().pfo_set_coherent(None, 0)
+        return
+    p = np.ascontiguousarray(partners, dtype=np.int32).reshape(-1, 2)
+    lib().pfo_set_coherent(_ptr(p), p.shape[0])
 
 
 def diffusion_substep(m: OModel, p: OParams, dt_sub, phase, conc1, conc2, C) -> None:

@@ -70,6 +70,7 @@ class PfModel(ctypes.Structure):
         ("avg_carbon", ctypes.c_int),
         ("drag", ctypes.c_int),
         ("drag_binding", ctypes.c_double), ("drag_vmax0", ctypes.c_double), ("drag_qsd", ctypes.c_double),
+        ("coherent", ctypes.c_int), ("coh_npp0", ctypes.c_int),
     ]
 
 
@@ -91,11 +92,12 @@ class PfStepParams(ctypes.Structure):
         ("k", _d9 * 2), ("c", _d9 * 2),
         ("df_model", ctypes.c_int),
         ("df_ratio", _d9), ("df_ref", ctypes.c_double),
-        ("avg_range", ctypes.c_int),
+        ("avg_range", ctypes.c_int), ("avg_conc", ctypes.c_int),
         ("drag_model", ctypes.c_int),
         ("drag_vmax", ctypes.c_double), ("drag_ex0", ctypes.c_double), ("drag_de_heat", ctypes.c_double),
         ("drag_de_cool", ctypes.c_double), ("drag_u0", ctypes.c_double),
         ("drag_corr", ctypes.c_double * 2), ("drag_drag0", ctypes.c_double * 2),
+        ("coh_model", ctypes.c_int), ("coh_npp0", ctypes.c_int),
     ]
 
 
@@ -160,6 +162,8 @@ SYMBOLS = {
     "pf_write_vti_binary": (_I, [_P, ctypes.c_char_p, _I, _I]),
     "pf_write_wait": (_I, [_P]),
     "pf_init_device": (_I, [_P, _P, _D]),
+    "pf_set_coherent_grains": (_I, [_P, _P, _I]),
+    "pf_init_coherent": (_I, [ctypes.POINTER(PfModel), ctypes.POINTER(PfInitSpec), _P]),
     "pf_write_vti_binary_host": (_I, [ctypes.c_char_p, _I, _I, _I, _I, _I, _D, _P, _P]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfModel), _I, ctypes.POINTER(_P)]),
     "pf_batch_upload": (_I, [_P, _I, _P, _P, _P, _P, _D]),
@@ -260,6 +264,14 @@ def init_microstructure_box(model: PfModel, spec: PfInitSpec, time: float, z0: i
     return st
 
 
+def init_coherent(model: PfModel, spec: PfInitSpec) -> np.ndarray:
+    """Coherent ferrite partners of the nuclei of spec (pf_init_coherent):
+    int32 [n_nuclei, 2], 0 = none."""
+    out = np.zeros(2 * max(spec.n_nuclei, 0), np.int32)
+    check(lib().pf_init_coherent(ctypes.byref(model), ctypes.byref(spec), _ptr(out)), "pf_init_coherent")
+    return out.reshape(-1, 2)
+
+
 class PhaseField:
     """Host-side mirror of the reference's ``phase_field`` object, running the
     whole time step on the GPU through libpfstep."""
@@ -293,6 +305,12 @@ class PhaseField:
     def upload(self, state: dict, time: float) -> None:
         check(lib().pf_upload_state(self._ctx, _ptr(state["ids"]), _ptr(state["phi"]), _ptr(state["phase"]),
                                     _ptr(state.get("conc")), _ptr(state["C"]), time), "pf_upload_state")
+
+    def set_coherent_grains(self, partners: np.ndarray) -> None:
+        """Coherent ferrite partners of austenite grains 200001, 200002, ...
+        (int32 [n, 2], 0 = none) for the coherent-grain mobility."""
+        p = np.ascontiguousarray(partners, dtype=np.int32).reshape(-1, 2)
+        check(lib().pf_set_coherent_grains(self._ctx, _ptr(p), p.shape[0]), "pf_set_coherent_grains")
 
     def construct_on_device(self, spec: PfInitSpec, time: float | None = None) -> None:
         """The seeded initial state generated on the GPU, straight into the

@@ -129,7 +129,10 @@ struct pf_ctx {
     double *phase = nullptr;
     double *conc[2] = {nullptr, nullptr};
     double *C = nullptr;
-    double *avg = nullptr;  // interface-averaged concentrations (models with avg_carbon)
+    double *avg = nullptr;  // interface-averaged concentrations (models with avg_carbon or coherent)
+    unsigned char *coh_flags = nullptr;  // Has_ferrite / Rex_intf per cell (models with coherent)
+    int *coh = nullptr;                  // coherent partners, 2 per austenite grain
+    int n_coh = 0;
     int cur = 0, curc = 0;
     // FP32 compact layout
     ushort4 *gid[2] = {nullptr, nullptr};
@@ -224,7 +227,7 @@ void free_all(pf_ctx *c) {
         cudaFree(c->ids[i]); cudaFree(c->phi[i]); cudaFree(c->conc[i]);
         cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
     }
-    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->avg); cudaFree(c->phase32);
+    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->avg); cudaFree(c->coh_flags); cudaFree(c->coh); cudaFree(c->phase32);
     cudaFree(c->d_span); cudaFree(c->d_trunc); cudaFree(c->rest); cudaFree(c->rest_count);
     cudaFree(c->st_ids); cudaFree(c->st_phi); cudaFree(c->st_phase); cudaFree(c->st_C); cudaFree(c->st_conc);
     cudaFree(c->partials); cudaFree(c->d_red);
@@ -243,7 +246,8 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         const int a = c->cur;
         e = timed(c, 0, [&] {
             return pf_launch_phase_f64(P, c->ids[a], c->phi[a], c->ids[1 - a], c->phi[1 - a], c->phase,
-                                       c->conc[c->curc], c->C, c->avg, c->stream);
+                                       c->conc[c->curc], c->C, c->avg, c->coh_flags, c->coh, c->n_coh,
+                                       c->stream);
         });
         if (e != cudaSuccess) return e;
         c->cur = 1 - a;
@@ -351,8 +355,10 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         return pf_fail(PF_ERR_ARG, "pf_create: bad model");
     if (precision == PF_PREC_FP32C && (long long)model->ix * model->iy * model->iz > 0xffffffffLL)
         return pf_fail(PF_ERR_RANGE, "pf_create: the compact FP32 path indexes cells with 32 bits");
-    if (precision == PF_PREC_FP32C && (model->avg_carbon || model->drag))
-        return pf_fail(PF_ERR_ARG, "pf_create: the interface-averaged carbon and the solute drag run on the FP64 path only");
+    if (precision == PF_PREC_FP32C && (model->avg_carbon || model->drag || model->coherent))
+        return pf_fail(PF_ERR_ARG,
+                       "pf_create: the interface-averaged carbon, the solute drag and the coherent-grain mobility run on "
+                       "the FP64 path only");
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
         cudaGetLastError();
@@ -379,7 +385,8 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         }
         alloc((void **)&c->phase, 3 * N * sizeof(double));
         alloc((void **)&c->C, N * c->nsol * sizeof(double));
-        if (model->avg_carbon) alloc((void **)&c->avg, 3 * N * sizeof(double));
+        if (model->avg_carbon || model->coherent) alloc((void **)&c->avg, 3 * N * sizeof(double));
+        if (model->coherent) alloc((void **)&c->coh_flags, N);
     } else {
         for (int i = 0; i < 2; i++) {
             alloc((void **)&c->gid[i], N * sizeof(ushort4));
@@ -425,6 +432,26 @@ extern "C" int pf_set_stream(pf_ctx *c, void *stream) {
         PF_CUDA_OK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         c->own_stream = true;
     }
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
+    return PF_OK;
+}
+
+extern "C" int pf_set_coherent_grains(pf_ctx *c, const int32_t *partners, int n_austenite) {
+    if (!c) return pf_fail(PF_ERR_ARG, "pf_set_coherent_grains: null context");
+    if (!c->model.coherent || c->prec != PF_PREC_FP64)
+        return pf_fail(PF_ERR_ARG, "pf_set_coherent_grains: the model has no coherent-grain mobility");
+    if (n_austenite < 0 || n_austenite > PF_MAXGRAIN_PER_PHASE || (n_austenite > 0 && !partners))
+        return pf_fail(PF_ERR_ARG, "pf_set_coherent_grains: bad table");
+    PF_CUDA_OK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->coh);
+    c->coh = nullptr;
+    c->n_coh = 0;
+    if (n_austenite > 0) {
+        PF_CUDA_OK(cudaMalloc((void **)&c->coh, 2 * (size_t)n_austenite * sizeof(int)));
+        PF_CUDA_OK(cudaMemcpy(c->coh, partners, 2 * (size_t)n_austenite * sizeof(int), cudaMemcpyHostToDevice));
+        c->n_coh = n_austenite;
+    }
+    // a captured step holds the old table's address
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; c->gphase = -1; }
     return PF_OK;
 }
@@ -801,8 +828,10 @@ extern "C" int pf_batch_create(const pf_model *models, int ndom, pf_batch **out)
         const pf_model &m = models[d];
         if (m.iz != 1) return pf_fail(PF_ERR_ARG, "pf_batch_create: batched domains are 2D (iz == 1)");
         if (m.nsol != models[0].nsol) return pf_fail(PF_ERR_ARG, "pf_batch_create: all domains need the same solutes");
-        if (m.avg_carbon || m.drag)
-            return pf_fail(PF_ERR_ARG, "pf_batch_create: the interface-averaged carbon and the solute drag run on the FP64 path only");
+        if (m.avg_carbon || m.drag || m.coherent)
+            return pf_fail(PF_ERR_ARG,
+                           "pf_batch_create: the interface-averaged carbon, the solute drag and the coherent-grain "
+                           "mobility run on the FP64 path only");
         for (int t = 1; t < m.nT; t++)
             if (m.T_temp[t] != m.T_temp[0])
                 return pf_fail(PF_ERR_ARG, "pf_batch_create: each domain needs a constant temperature");

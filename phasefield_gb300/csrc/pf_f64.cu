@@ -59,16 +59,24 @@ __device__ __forceinline__ void pf_partition(double C, const double ph[3], const
 // and elsewhere, the cell's own concentrations.  The Fortran loop updates the
 // phase fractions in place as it goes (an order the OpenMP schedule decides);
 // here every cell reads the values of the start of the sweep.
+// flags (may be null): the same scan's Has_ferrite (bit 0: a cell of the line
+// holds ferrite above 1 - cutoff) and Rex_intf (bit 1: a cell of the line with
+// both phases above the cutoff holds a ferrite grain of the initial class,
+// id <= coh_npp0, and a recrystallised one), sparse.f90:214-222; 0 outside
+// Flag_coexist(2).
 __global__ void __launch_bounds__(256) k_avg_conc_f64(const __grid_constant__ pf_step_params P,
+                                                      const int *__restrict__ ids1,
                                                       const double *__restrict__ phase,
                                                       const double *__restrict__ conc1,
-                                                      double *__restrict__ avg) {
+                                                      double *__restrict__ avg,
+                                                      unsigned char *__restrict__ flags) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     const int ix = P.ix, iy = P.iy, iz = P.iz;
     const double cutoff = P.cutoff;
     double out[3] = {conc1[3 * n], conc1[3 * n + 1], conc1[3 * n + 2]};
+    int fl = 0;
     auto at = [&](int i, int j, int k) { return (long long)i + (long long)ix * (j + (long long)iy * k); };
     auto ph1 = [&](int i, int j, int k) { return phase[3 * at(i, j, k)]; };
     if (phase[3 * n] > cutoff && phase[3 * n + 1] > cutoff) {
@@ -84,6 +92,9 @@ __global__ void __launch_bounds__(256) k_avg_conc_f64(const __grid_constant__ pf
         const int R = P.avg_range;
         const int rz = min((iz - 1) / 2, R), ry = min((iy - 1) / 2, R), rx = min((ix - 1) / 2, R);
         double sum[3] = {0., 0., 0.}, num = 0.;
+        bool has_ferrite = false, rex = false;
+        const double bulk = 1. - cutoff;
+        const int npp0 = P.coh_npp0;
         for (int kk = -rz; kk <= rz; kk++) {
             const int z = pf_mod(ck + kk, iz);
             for (int jj = -ry; jj <= ry; jj++) {
@@ -95,7 +106,20 @@ __global__ void __launch_bounds__(256) k_avg_conc_f64(const __grid_constant__ pf
                     if (dist > g2 * 1.0) continue;
                     const long long m = at(x, y, z);
                     const double p1 = phase[3 * m], p2 = phase[3 * m + 1];
+                    if (p1 > bulk) has_ferrite = true;
                     if (p1 < cutoff || p2 < cutoff) continue;
+                    if (flags) {
+                        bool lo = false, hi = false;
+#pragma unroll
+                        for (int a = 0; a < 6; a++) {
+                            const int g = ids1[6 * m + a];
+                            if (pf_phase_of_grain(g) == 1) {
+                                if (g <= npp0) lo = true;
+                                else hi = true;
+                            }
+                        }
+                        rex = rex || (lo && hi);
+                    }
                     const double h0 = ph1(pf_wrap(x, ix, 1), y, z) - ph1(pf_wrap(x, ix, -1), y, z);
                     const double h1 = ph1(x, pf_wrap(y, iy, 1), z) - ph1(x, pf_wrap(y, iy, -1), z);
                     const double h2 = ph1(x, y, pf_wrap(z, iz, 1)) - ph1(x, y, pf_wrap(z, iz, -1));
@@ -117,15 +141,27 @@ __global__ void __launch_bounds__(256) k_avg_conc_f64(const __grid_constant__ pf
             out[1] = sum[1] / num;
             out[2] = sum[2] / num;
         }
+        fl = (has_ferrite ? 1 : 0) | (rex ? 2 : 0);
     }
+    if (flags) flags[n] = (unsigned char)fl;
     avg[3 * n] = out[0];
     avg[3 * n + 1] = out[1];
     avg[3 * n + 2] = out[2];
 }
 
+// Whether austenite grain 'aus' nucleated coherent with ferrite grain 'fer'
+// (Coherent_grain(aus, :) holds fer): coh[2k], coh[2k+1] for aus = 200001 + k.
+__device__ __forceinline__ bool pf_coh_has(const int *coh, int n_coh, int aus, int fer) {
+    const int k = aus - (2 * PF_MAXGRAIN_PER_PHASE + 1);
+    if (k < 0 || k >= n_coh || fer == 0) return false;
+    return coh[2 * k] == fer || coh[2 * k + 1] == fer;
+}
+
 // Phase_field_solver (solver.cpp:147-304), one thread per cell.  avg (may be
 // null): the phase concentrations the driving force reads instead of the
-// cell's own (k_avg_conc_f64).
+// cell's own (k_avg_conc_f64), when P.avg_conc is set.  flags, coh (null
+// unless P.coh_model): the scan's Has_ferrite / Rex_intf bits and the
+// coherent-partner table of the Fortran model's coherent-grain mobility.
 __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P,
                                                    const int *__restrict__ ids1,
                                                    const double *__restrict__ phi1,
@@ -133,7 +169,9 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                                                    double *__restrict__ phase,
                                                    double *__restrict__ conc1,
                                                    const double *__restrict__ C,
-                                                   const double *__restrict__ avg) {
+                                                   const double *__restrict__ avg,
+                                                   const unsigned char *__restrict__ flags,
+                                                   const int *__restrict__ coh, int n_coh) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
@@ -231,7 +269,7 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
     // Driving forces depend only on the phase pair and the cell's carbon
     // concentration (solver.cpp:231-232, 374-387): evaluate the six ordered
     // off-diagonal pairs once.
-    const double *lcp = avg ? avg : conc1;
+    const double *lcp = (avg && P.avg_conc) ? avg : conc1;
     double lc[3];
     lc[0] = lcp[3 * n + 0]; lc[1] = lcp[3 * n + 1]; lc[2] = lcp[3 * n + 2];
     double df[9];
@@ -241,6 +279,19 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
         for (int b = 1; b <= 3; b++) df[(a - 1) + 3 * (b - 1)] = pf_df(P, a, b, lc[a - 1], lc[b - 1]);
 
     const double factor1 = P.factor1, factor2 = P.factor2, factor3 = P.factor3;
+    // sparse.f90:300-306: the coherent-mobility gate of the cell -- the scan
+    // saw bulk ferrite and no recrystallisation front, and exactly one of the
+    // cell's own grains above the cutoff (Ind_ph1(1:N_nonzero)) is ferrite.
+    bool coh_cell = false;
+    if (P.coh_model && flags && coh) {
+        const int fl = flags[n];
+        int nown = 0, nfer = 0;
+#pragma unroll
+        for (int a = 0; a < 6; a++) nown += own_v[a] > cutoff ? 1 : 0;
+#pragma unroll
+        for (int a = 0; a < 6; a++) nfer += (a < nown && pf_phase_of_grain(own_id[a]) == 1) ? 1 : 0;
+        coh_cell = (fl & 1) && !(fl & 2) && nfer == 1;
+    }
     double del[PF_NSTENCIL];
     double drag[PF_NSTENCIL];  // sum over ferrite/austenite partners of m_ij f3 sqrt(phi_i phi_j) (solute drag)
 #pragma unroll
@@ -264,9 +315,13 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                         for (int t = 0; t < 9; t++)
                             if (t == e) dfe = df[t];
                         d += factor3 * sqrt(s1[ii] * s1[jj]) * dfe;
-                        d *= P.m[e];
+                        // sparse.f90:298-315: 0.02 of the mobility for a coherent pair
+                        const bool cp = coh_cell && ((pi == 2 && pf_coh_has(coh, n_coh, sid[ii], sid[jj])) ||
+                                                     (pj == 2 && pf_coh_has(coh, n_coh, sid[jj], sid[ii])));
+                        const double mob = cp ? 0.02 * P.m[e] : P.m[e];
+                        d = cp ? mob * d : d * mob;
                         del[ii] += d;
-                        if (P.drag_model && pi + pj == 3) drag[ii] += P.m[e] * (factor3 * sqrt(s1[ii] * s1[jj]));
+                        if (P.drag_model && pi + pj == 3) drag[ii] += mob * (factor3 * sqrt(s1[ii] * s1[jj]));
                     }
                 }
             }
@@ -464,15 +519,18 @@ inline unsigned pf_blocks(long long N, int threads) { return (unsigned)((N + thr
 
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
                                 double *phi2, double *phase, double *conc1, const double *C, double *avg,
-                                cudaStream_t s) {
-    const bool averaged = P.avg_range > 0 && avg;
-    if (averaged) {
-        k_avg_conc_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, phase, conc1, avg);
+                                unsigned char *flags, const int *coh, int n_coh, cudaStream_t s) {
+    const bool scanned = P.avg_range > 0 && avg;
+    const bool coherent = scanned && P.coh_model && flags && coh;
+    if (scanned) {
+        k_avg_conc_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, ids1, phase, conc1, avg,
+                                                                                  coherent ? flags : nullptr);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, ids1, phi1, ids2, phi2, phase, conc1, C,
-                                                                           averaged ? avg : nullptr);
+    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(
+        P, ids1, phi1, ids2, phi2, phase, conc1, C, scanned ? avg : nullptr, coherent ? flags : nullptr,
+        coherent ? coh : nullptr, n_coh);
     return cudaGetLastError();
 }
 

@@ -78,6 +78,8 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
     m->avg_carbon = 0;
     m->drag = 0;
     m->drag_binding = m->drag_vmax0 = m->drag_qsd = 0.;
+    m->coherent = 0;
+    m->coh_npp0 = 0;
     {
         std::string word;
         f >> word;
@@ -95,6 +97,10 @@ extern "C" int pf_thermo_read(const char *path, pf_model *m) {
                     if (!(ls >> m->drag_binding >> m->drag_vmax0 >> m->drag_qsd) || !(m->drag_vmax0 > 0.))
                         return pf_fail(PF_ERR_IO, "thermo file: SOLUTE_DRAG needs binding energy, v_max0 > 0, Q_sd");
                     m->drag = 1;
+                } else if (kw == "COHERENT_MOBILITY") {  // last id of the initial ferrite class (Npp0)
+                    if (!(ls >> m->coh_npp0) || m->coh_npp0 < 0)
+                        return pf_fail(PF_ERR_IO, "thermo file: COHERENT_MOBILITY needs npp0 >= 0");
+                    m->coherent = 1;
                 } else return pf_fail(PF_ERR_IO, "thermo file: unknown keyword " + kw);
             }
             return PF_OK;
@@ -409,7 +415,10 @@ void pf_compute_params(const pf_model &m, double time, pf_step_params &p) {
         }
     p.pfm_dt = m.dx * m.dx / dims * 0.2 / maxms;
     p.diff_dt = m.dx * m.dx / maxD / dims * 0.2;
-    p.avg_range = m.avg_carbon ? m.i_intf + 1 : 0;  // sparse.f90:186
+    p.avg_range = (m.avg_carbon || m.coherent) ? m.i_intf + 1 : 0;  // sparse.f90:186
+    p.avg_conc = m.avg_carbon ? 1 : 0;
+    p.coh_model = m.coherent ? 1 : 0;
+    p.coh_npp0 = m.coh_npp0;
     if (m.thermo_model == 1) {
         pf_f90_thermo(T, p);
         if (m.drag) pf_f90_drag(m, T, p);
@@ -573,4 +582,12 @@ extern "C" int pf_init_microstructure_box(const pf_model *model, const pf_init_s
     const int st = pf_init_state(model->ix, model->iy, model->iz, model->nsol, model->cutoff, spec, &P.k[0][0],
                                  &P.c[0][0], z0, nz, ids, phi, phase, conc, C, &msg);
     return st == PF_OK ? PF_OK : pf_fail(st, std::string("pf_init_microstructure: ") + (msg ? msg : "failed"));
+}
+
+extern "C" int pf_init_coherent(const pf_model *model, const pf_init_spec *spec, int32_t *partners) {
+    if (!model || !spec) return pf_fail(PF_ERR_ARG, "pf_init_coherent: null argument");
+    const char *msg = nullptr;
+    const int st = pf_init_coherent_table(model->ix, model->iy, model->iz, model->nsol, model->cutoff, spec, partners,
+                                          &msg);
+    return st == PF_OK ? PF_OK : pf_fail(st, std::string("pf_init_coherent: ") + (msg ? msg : "failed"));
 }

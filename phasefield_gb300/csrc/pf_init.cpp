@@ -153,3 +153,44 @@ extern "C" int pf_init_state(int ix, int iy, int iz, int nsol, double cutoff, co
     if (msg) *msg = nullptr;
     return PF_OK;
 }
+
+extern "C" int pf_init_coherent_table(int ix, int iy, int iz, int nsol, double cutoff, const pf_init_spec *spec,
+                                      int32_t *partners, const char **msg) {
+    auto fail = [&](int st, const char *m) {
+        if (msg) *msg = m;
+        return st;
+    };
+    if (!spec || (spec->n_nuclei > 0 && !partners)) return fail(PF_ERR_ARG, "null argument");
+    PfInitHost H;
+    const int st = pf_init_prepare(ix, iy, iz, nsol, cutoff, spec, H, msg);
+    if (st != PF_OK) return st;
+    // The matrix before nucleation: the same set-up with no nucleus near any cell.
+    const std::vector<double> none;
+    PfHostBuckets empty;
+    const int blen[3] = {ix, iy, iz};
+    empty.build(none, none, none, blen, 1.0);
+    pfinit::Setup S = H.S;
+    S.bnuc = empty.view(empty.start.data(), empty.items.data());
+    auto site = [](double v, int L) {
+        const long long c = (long long)std::floor(v + 0.5);
+        return (int)(((c % L) + L) % L);
+    };
+    int crowded = 0;
+#pragma omp parallel for schedule(static) reduction(| : crowded)
+    for (int n = 0; n < spec->n_nuclei; n++) {
+        const int i = site(H.nx[n], ix), j = S.yflat ? 0 : site(H.ny[n], iy), k = S.zflat ? 0 : site(H.nz[n], iz);
+        int32_t ids[6];
+        double phi[6], ph[3], Cv[2];
+        if (!pfinit::cell(S, i, j, k, ids, phi, ph, Cv)) crowded = 1;
+        int fer[6], nf = 0;
+        for (int a = 0; a < 6; a++)
+            if (ids[a] / pfinit::kGrainsPerPhase == 1) fer[nf++] = ids[a];
+        std::sort(fer, fer + nf, [](int a, int b) { return a > b; });
+        const int or_num = std::min(2, nf - 1);
+        partners[2 * n] = or_num >= 1 ? fer[0] : 0;
+        partners[2 * n + 1] = or_num >= 2 ? fer[1] : 0;
+    }
+    if (crowded) return fail(PF_ERR_RANGE, "more than 256 inclusions near one cell");
+    if (msg) *msg = nullptr;
+    return PF_OK;
+}

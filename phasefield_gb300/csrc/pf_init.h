@@ -21,6 +21,13 @@ int pf_init_state(int ix, int iy, int iz, int nsol, double cutoff, const pf_init
                   const double *c, int z0, int nz, int32_t *ids, double *phi, double *phase, double *conc,
                   double *C, const char **msg);
 
+/* Coherent partners of the nuclei of spec (module_nucleation.f90:357-367,
+ * nucleation in a grain boundary): at the cell nearest nucleus n, evaluated
+ * without any nucleus, Or_num = min(2, ferrite grains there - 1) partners, the
+ * largest ferrite ids first; partners[2n], partners[2n+1] (0: none). */
+int pf_init_coherent_table(int ix, int iy, int iz, int nsol, double cutoff, const pf_init_spec *spec,
+                           int32_t *partners, const char **msg);
+
 #ifdef __cplusplus
 }
 #endif

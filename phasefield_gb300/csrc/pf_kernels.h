@@ -5,10 +5,12 @@
 
 // ---- FP64 reference layout (pf_f64.cu) ----
 // avg: 3N doubles of scratch for the interface-averaged concentrations
-// (used when P.avg_range > 0; may be null otherwise).
+// (used when P.avg_range > 0; may be null otherwise).  flags: N bytes of
+// scratch for the coherent-mobility flags, coh: the coherent-partner table of
+// n_coh austenite grains (used when P.coh_model; may be null otherwise).
 cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const double *phi1, int *ids2,
                                 double *phi2, double *phase, double *conc1, const double *C, double *avg,
-                                cudaStream_t s);
+                                unsigned char *flags, const int *coh, int n_coh, cudaStream_t s);
 // 1 if a solute-drag velocity iteration of the FP64 sweep found no root since
 // the last call (then cleared).
 int pf_drag_take_failure();

@@ -81,14 +81,20 @@ THERMO_F90_TEXT = """F90_POLYNOMIAL
 F90_DRAG_LINE = "SOLUTE_DRAG 10000. 1.0e11 247650.\n"
 
 
-def write_thermo(path: str, model: str = "linear") -> str:
+def write_thermo(path: str, model: str = "linear", coherent_npp0: int | None = None) -> str:
     """model: "linear" (the reference's sample lines), "f90" (the Fortran
     model's thermodynamics), "f90avg" (that, plus the interface-averaged
     carbon of sparse.f90:184-255) or "f90drag" (that, plus the solute drag of
-    sparse.f90:326-360 with the Fortran sample's parameters)."""
+    sparse.f90:326-360 with the Fortran sample's parameters).  coherent_npp0
+    (an "f90" model): add the coherent-grain mobility of sparse.f90:298-315,
+    ferrite ids up to coherent_npp0 forming the initial class."""
     text = {"linear": THERMO_TEXT, "f90": THERMO_F90_TEXT,
             "f90avg": THERMO_F90_TEXT + "AVERAGED_INTERFACE_CARBON\n",
             "f90drag": THERMO_F90_TEXT + F90_DRAG_LINE}[model]
+    if coherent_npp0 is not None:
+        if model == "linear":
+            raise ValueError("the coherent-grain mobility is an option of the Fortran model's thermodynamics")
+        text += f"COHERENT_MOBILITY {int(coherent_npp0)}\n"
     with open(path, "w") as f:
         f.write(text)
     return path

@@ -73,3 +73,23 @@ def ref_cpu_case(tmpdir: str, golden, name: str):
     exp["fraction"] = str(golden[f"{name}_fraction"])
     exp["vti"] = str(golden[f"{name}_vti"]) if f"{name}_vti" in golden.files else None
     return cfg, st0, exp
+
+
+def adjacent_partners(ids, phi, n_nuclei, cutoff):
+    """A coherent-partner table that makes every nucleus coherent with the
+    (up to two largest) ferrite grains it shares a cell with in 'ids' -- a
+    table under which the coherent mobility acts on most interfaces."""
+    I = ids.reshape(-1, 6)
+    V = phi.reshape(-1, 6)
+    sets = [set() for _ in range(n_nuclei)]
+    for row, val in zip(I, V):
+        live = [int(g) for g, v in zip(row, val) if v > cutoff]
+        fer = [g for g in live if g // 100000 == 1]
+        for g in live:
+            if g // 100000 == 2 and g - 200001 < n_nuclei:
+                sets[g - 200001].update(fer)
+    out = np.zeros((n_nuclei, 2), np.int32)
+    for n, s_ in enumerate(sets):
+        top = sorted(s_, reverse=True)[:2]
+        out[n, : len(top)] = top
+    return out

@@ -12,6 +12,7 @@ import pytest
 
 import phasefield_gb300 as pf
 import pyoracle as po
+from helpers import adjacent_partners
 from phasefield_gb300 import workloads as W
 
 
@@ -104,13 +105,21 @@ def test_adjoint_rejects_f90_thermodynamics(tmp_path):
     assert pf.lib().pf_adj_create(pf.ctypes.byref(m), pf.PF_PREC_FP64, 10, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
 
 
-def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf):
+def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf, ids=None, npp0=0):
     """sparse.f90:141-146 and 184-255 written out literally (1-based indices,
-    MYNGB of util_func.f90:33-47), on the values of the start of the sweep."""
+    MYNGB of util_func.f90:33-47), on the values of the start of the sweep.
+    With ids: also Has_ferrite (bit 0) and Rex_intf (bit 1) of every cell
+    (sparse.f90:137-139, 214-222; PHASE_INDEX of util_func.f90:50-60 on this
+    model's ids: ferrite 1000xx, austenite 2000xx, cementite 3000xx)."""
     ix, iy, iz = grid
     ph = phase.reshape(iz, iy, ix, 3)
     cc = conc.reshape(iz, iy, ix, 3)
     out = cc.copy()
+    flags = np.zeros((iz, iy, ix), np.uint8)
+    ind = None if ids is None else ids.reshape(iz, iy, ix, 6)
+
+    def phase_index(g):
+        return -10000 if g <= 0 else g // 100000
 
     def myngb(coord, lcoord, n):
         nn = n % lcoord
@@ -134,6 +143,7 @@ def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf):
                 for g in grad:
                     g2 += g * g
                 num, acc = 0., [0., 0., 0.]
+                has_ferrite = rex_intf = False
                 for Kk in range(-min((iz - 1) // 2, rng_), min((iz - 1) // 2, rng_) + 1):
                     Iiz = myngb(K, iz, Kk)
                     for Jj in range(-min((iy - 1) // 2, rng_), min((iy - 1) // 2, rng_) + 1):
@@ -145,8 +155,14 @@ def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf):
                             c = Ii * grad[1] - Jj * grad[0]
                             if a * a + b * b + c * c > g2 * 1.0:
                                 continue
+                            if vp(1, Iix, Iiy, Iiz) > 1. - cutoff:
+                                has_ferrite = True
                             if vp(1, Iix, Iiy, Iiz) < cutoff or vp(2, Iix, Iiy, Iiz) < cutoff:
                                 continue
+                            if ind is not None:
+                                lst = [int(g) for g in ind[Iiz - 1, Iiy - 1, Iix - 1]]
+                                rex_intf = rex_intf or (any(phase_index(g) == 1 and g <= npp0 for g in lst) and
+                                                        any(phase_index(g) == 1 and g > npp0 for g in lst))
                             h = [vp(1, myngb(Iix, ix, 1), Iiy, Iiz) - vp(1, myngb(Iix, ix, -1), Iiy, Iiz),
                                  vp(1, Iix, myngb(Iiy, iy, 1), Iiz) - vp(1, Iix, myngb(Iiy, iy, -1), Iiz),
                                  vp(1, Iix, Iiy, myngb(Iiz, iz, 1)) - vp(1, Iix, Iiy, myngb(Iiz, iz, -1))]
@@ -163,7 +179,8 @@ def _avg_fortran_literal(phase, conc, grid, cutoff, i_intf):
                             num += 1.
                 if num > 0.:
                     out[K - 1, J - 1, I - 1] = [a_ / num for a_ in acc]
-    return out.ravel()
+                flags[K - 1, J - 1, I - 1] = int(has_ferrite) | (int(rex_intf) << 1)
+    return out.ravel() if ids is None else (out.ravel(), flags.ravel())
 
 
 @pytest.mark.parametrize("grid", [(24, 20, 1), (10, 9, 8)])
@@ -311,3 +328,118 @@ def test_solute_drag_keyword_and_precision(tmp_path):
         pf.read_model(cfg)
     h = pf.ctypes.c_void_p()
     assert pf.lib().pf_create(pf.ctypes.byref(m), pf.PF_PREC_FP32C, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
+
+
+def _coh_case(tmp_path, grid, model="f90", npp0=0, T=1023.0):
+    W.write_thermo(str(tmp_path / "thermo_coh.txt"), model, coherent_npp0=npp0)
+    cfg = W.write_config(str(tmp_path / "coh.txt"), grid=grid, T=T, thermo_file="thermo_coh.txt",
+                         directory=str(tmp_path / "out"))
+    return pf.read_model(cfg), po.load_model(cfg)
+
+
+@pytest.mark.parametrize("grid,npp0", [((24, 20, 1), 0), ((24, 20, 1), 100002), ((10, 9, 8), 100001)])
+def test_coherent_flags_oracle_equal_fortran_literal(tmp_path, grid, npp0):
+    """The scan's Has_ferrite / Rex_intf flags and the averaged carbon of the
+    oracle equal a literal 1-based restatement of sparse.f90:137-139, 184-255."""
+    m, om = _coh_case(tmp_path, grid, npp0=npp0)
+    assert m.coherent == 1 and om.coherent == 1 and m.coh_npp0 == npp0
+    p, q = pf.params_at(m, 0.0), po.params_at(om, 0.0)
+    assert (p.avg_range, p.avg_conc, p.coh_model, p.coh_npp0) == (m.i_intf + 1, 0, 1, npp0)
+    assert (q.avg_range, q.avg_conc, q.coh_model, q.coh_npp0) == (p.avg_range, 0, 1, npp0)
+    spec = W.WORKLOADS["3d256"].spec()
+    spec.n_grains, spec.n_nuclei, spec.nucleus_radius = 4, 4, 2.5
+    st = po.init_state(om, spec, 0.0)
+    N = grid[0] * grid[1] * grid[2]
+    conc = np.zeros(3 * N * om.nsol)
+    po.partition_all(om, q, st["phase"], st["C"], conc)
+    conc = conc[: 3 * N]
+    got, fl = po.avg_conc(om, q, st["phase"], conc, ids=st["ids"], with_flags=True)
+    want, wfl = _avg_fortran_literal(st["phase"], conc, grid, om.cutoff, om.i_intf, ids=st["ids"], npp0=npp0)
+    assert np.array_equal(got, want)
+    assert np.array_equal(fl, wfl)
+    assert (fl & 1).any()
+    if npp0:
+        assert (fl & 2).any()
+
+
+def _splitmix64(s):
+    M = (1 << 64) - 1
+    s = (s + 0x9E3779B97F4A7C15) & M
+    z = s
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return s, z ^ (z >> 31)
+
+
+@pytest.mark.parametrize("grid", [(40, 36, 1), (16, 14, 12)])
+def test_init_coherent_follows_boundary_nucleation_rule(tmp_path, grid):
+    """pf_init_coherent: at the cell nearest each nucleus of the matrix
+    without nuclei, Or_num = min(2, ferrite grains - 1) partners, the largest
+    ferrite ids (module_nucleation.f90:357-367).  Nucleus positions are
+    re-drawn here from the generator's seed stream (grains first, then
+    nuclei, three uniforms each)."""
+    m, _ = _coh_case(tmp_path, grid)
+    spec = W.WORKLOADS["3d256"].spec()
+    spec.n_grains, spec.n_nuclei, spec.n_particles, spec.nucleus_radius = 6, 40, 0, 2.0
+    got = pf.init_coherent(m, spec)
+    assert got.shape == (40, 2)
+    spec0 = W.WORKLOADS["3d256"].spec()
+    spec0.n_grains, spec0.n_nuclei, spec0.n_particles, spec0.nucleus_radius = 6, 0, 0, 2.0
+    matrix = pf.init_microstructure(m, spec0, 0.0)
+    ix, iy, iz = grid
+    I = matrix["ids"].reshape(iz, iy, ix, 6)
+    s = spec.seed
+    draws = []
+    for _ in range(3 * (spec.n_grains + spec.n_nuclei)):
+        s, z = _splitmix64(s)
+        draws.append((z >> 11) * (1.0 / 9007199254740992.0))
+    nuc = np.array(draws[3 * spec.n_grains:]).reshape(-1, 3) * [ix, iy, iz]
+    n_two = n_one = 0
+    for n, (x, y, z) in enumerate(nuc):
+        i = int(np.floor(x + 0.5)) % ix
+        j = 0 if iy == 1 else int(np.floor(y + 0.5)) % iy
+        k = 0 if iz == 1 else int(np.floor(z + 0.5)) % iz
+        fer = sorted((int(g) for g in I[k, j, i] if g // 100000 == 1), reverse=True)
+        or_num = min(2, len(fer) - 1)
+        want = [fer[0] if or_num >= 1 else 0, fer[1] if or_num >= 2 else 0]
+        assert list(got[n]) == want, n
+        n_two += or_num >= 2
+        n_one += or_num == 1
+    assert n_one + n_two > 0
+
+
+def test_coherent_keyword_and_precision(tmp_path):
+    (tmp_path / "bad.txt").write_text("F90_POLYNOMIAL\nCOHERENT_MOBILITY\n")
+    cfg = W.write_config(str(tmp_path / "c_bad.txt"), grid=(8, 8, 1), thermo_file="bad.txt",
+                         directory=str(tmp_path / "out"))
+    with pytest.raises(pf.PfError):
+        pf.read_model(cfg)
+    with pytest.raises(ValueError):
+        W.write_thermo(str(tmp_path / "t.txt"), "linear", coherent_npp0=0)
+    m, _ = _coh_case(tmp_path, (8, 8, 1))
+    h = pf.ctypes.c_void_p()
+    assert pf.lib().pf_create(pf.ctypes.byref(m), pf.PF_PREC_FP32C, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
+    ms = (pf.PfModel * 1)(m)
+    assert pf.lib().pf_batch_create(ms, 1, pf.ctypes.byref(h)) == pf.PF_ERR_ARG
+
+
+def test_coherent_mobility_changes_the_oracle_step(tmp_path):
+    """With every nucleus coherent with its neighbouring ferrite grains the
+    oracle slows those interfaces: the state differs from the same steps
+    without the table, and with a recrystallisation front everywhere
+    (every ferrite grain of the other class) it differs again."""
+    grid = (48, 40, 1)
+    m, om = _coh_case(tmp_path, grid)
+    spec = W.WORKLOADS["2d256"].spec()
+    spec.n_grains, spec.n_nuclei = 4, 5
+    st0 = po.init_state(om, spec, 0.0)
+    table = adjacent_partners(st0["ids"], st0["phi"], spec.n_nuclei, om.cutoff)
+    assert (table > 0).any()
+    runs = []
+    for tab in (table, None):
+        po.set_coherent(tab)
+        st = {k: v.copy() for k, v in st0.items()}
+        po.run(om, st, 0.0, 8)
+        runs.append(st)
+    po.set_coherent(None)
+    assert not np.array_equal(runs[0]["phi"], runs[1]["phi"])

@@ -11,7 +11,7 @@ import pytest
 
 import phasefield_gb300 as pf
 import pyoracle as po
-from helpers import copy_state, rel_maxnorm
+from helpers import adjacent_partners, copy_state, rel_maxnorm
 from phasefield_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -114,3 +114,47 @@ def test_f90_solute_drag_fp64_matches_oracle(gpu, tmp_path, grid, T):
                           directory=str(tmp_path / "out"))
     po.run(po.load_model(cfg2), plain, 0.0, 6)
     assert not np.array_equal(plain["phi"], ref["phi"])
+
+
+@pytest.mark.parametrize("grid,model,npp0", [((48, 40, 1), "f90", 0), ((16, 14, 12), "f90drag", 0),
+                                             ((40, 36, 1), "f90avg", 100002)])
+def test_f90_coherent_mobility_fp64_matches_oracle(gpu, tmp_path, grid, model, npp0):
+    """The coherent-grain mobility (sparse.f90:298-315) on the FP64 path, alone,
+    with the solute drag and with the averaged carbon plus a recrystallisation
+    class split: every field bit for bit equal to the oracle after six steps
+    under a table that makes each nucleus coherent with its neighbouring
+    ferrite grains, and different from the same steps without the table."""
+    W.write_thermo(str(tmp_path / "thermo_coh.txt"), model, coherent_npp0=npp0)
+    cfg = W.write_config(str(tmp_path / "coh.txt"), grid=grid, T=1023.0, thermo_file="thermo_coh.txt",
+                         directory=str(tmp_path / "out"))
+    m, om = pf.read_model(cfg), po.load_model(cfg)
+    assert m.coherent == 1
+    spec = W.WORKLOADS["3d256"].spec()
+    spec.n_grains, spec.n_nuclei, spec.nucleus_radius = 4, 5, 3.0
+    st0 = pf.init_microstructure(m, spec, 0.0)
+    table = adjacent_partners(st0["ids"], st0["phi"], spec.n_nuclei, m.cutoff)
+    assert (table > 0).any()
+    ref = copy_state(st0)
+    po.set_coherent(table)
+    po.drag_failures()
+    t_ref = po.run(om, ref, 0.0, 6)
+    po.set_coherent(None)
+    assert po.drag_failures() == 0
+    F = pf.PhaseField(m, pf.PF_PREC_FP64)
+    F.set_coherent_grains(table)
+    F.upload(st0, 0.0)
+    F.update(6)
+    F.synchronize()
+    got = F.download()
+    # the same steps without the table
+    F.set_coherent_grains(np.zeros((0, 2), np.int32))
+    F.upload(st0, 0.0)
+    F.update(6)
+    plain = F.download()
+    F.close()
+    assert got["time"] == t_ref
+    assert np.array_equal(got["ids"], ref["ids"])
+    for k in ("phi", "phase", "conc", "C"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert not np.array_equal(plain["phi"], got["phi"])
+
