@@ -310,8 +310,11 @@ int pf_batch_destroy(pf_batch *b);
  * J[1] = mean austenite carbon (sum phi_2 c_2 / sum phi_2) at the end.
  * pf_adj_gradient(objective 0 or 1) then returns dJ/ds by the hand-written
  * reverse sweep (segments recomputed from the checkpoints, discrete decisions
- * of every step held fixed).  pf_adj_timings: ms of the last forward and of
- * the last gradient (recomputation included). */
+ * of every step held fixed).  checkpoint_every = 0 is the record mode: the
+ * forward keeps every step's record on the device ((72 + 4*n_sub) bytes per
+ * cell and step in FP32, (136 + 8*n_sub) in FP64; PF_ERR_NOMEM when it does
+ * not fit) and the gradient only sweeps backwards.  pf_adj_timings: ms of the last forward and of the last gradient
+ * (recomputation included). */
 typedef struct pf_adj pf_adj;
 int pf_adj_create(const pf_model *model, int precision, int checkpoint_every, pf_adj **out);
 int pf_adj_upload(pf_adj *a, const int32_t *ids, const double *phi, const double *phase, const double *C,

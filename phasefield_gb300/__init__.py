@@ -497,7 +497,9 @@ class Batch:
 
 
 class Adjoint:
-    """Forward + hand-written adjoint of the compact step (pf_adj_*)."""
+    """Forward + hand-written adjoint of the compact step (pf_adj_*).
+    checkpoint_every = 0: record mode (every step kept by the forward, the
+    gradient without recomputation)."""
 
     def __init__(self, model: PfModel, precision: int = PF_PREC_FP64, checkpoint_every: int = 100):
         self.model = model

@@ -7,7 +7,9 @@ D_Mn) applied to the model's parameters; the output is the chosen objective at
 the end of ``nsteps`` steps (0: mean ferrite fraction, 1: mean austenite
 carbon).  Time step and sub-step count stay those of s = 1.
 
-    A = phasefield_gb300.Adjoint(model, PF_PREC_FP32C, checkpoint_every=100)
+    # checkpoint_every=0: record mode (the trajectory kept in HBM, no
+    # recomputation); a positive interval when it does not fit
+    A = phasefield_gb300.Adjoint(model, PF_PREC_FP32C, checkpoint_every=0)
     A.upload(state, 0.0)
     s = torch.ones(4, dtype=torch.float64, requires_grad=True)
     J = StepObjective.apply(s, A, 2000, 1)

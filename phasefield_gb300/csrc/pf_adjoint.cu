@@ -680,6 +680,16 @@ struct AdjCtx : pf_adj_impl {
     // segment storage: per step pre-step state and pre-sub-step carbon
     std::vector<ushort4 *> sg_gid;
     std::vector<R *> sg_phi, sg_ph, sg_C, sg_Csub;  // sg_Csub: each step's diffusion record
+    // Record mode (checkpoint_every = 0): the forward keeps every step's
+    // record, slices of one arena, and the gradient only sweeps backwards.
+    bool record = false;
+    char *arena = nullptr;
+    int arena_steps = 0;
+    std::vector<ushort4 *> rg_gid;
+    std::vector<R *> rg_phi, rg_ph, rg_C, rg_Csub;
+    cudaGraphExec_t rec_fwd = nullptr, rec_bwd = nullptr;
+    int rec_fwd_steps = -1, rec_bwd_steps = -1;
+    R *rb_C = nullptr, *rb_phi = nullptr, *rb_ph = nullptr;  // adjoint buffer roles at the reverse capture
     R *dscr = nullptr;  // the step planes of a forward run without records (9N)
     ushort4 *w_gid = nullptr, *v_gid = nullptr;  // w_*, v_*: the forward's two state sets
     R *w_phi = nullptr, *w_ph = nullptr, *w_C = nullptr, *w_C2 = nullptr;
@@ -710,6 +720,49 @@ struct AdjCtx : pf_adj_impl {
         for (auto &g : fwd_graph)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         if (seg_graph) { cudaGraphExecDestroy(seg_graph); seg_graph = nullptr; }
+        if (rec_fwd) { cudaGraphExecDestroy(rec_fwd); rec_fwd = nullptr; }
+        if (rec_bwd) { cudaGraphExecDestroy(rec_bwd); rec_bwd = nullptr; }
+        rec_fwd_steps = rec_bwd_steps = -1;
+    }
+
+    // Bytes of one step's record: pre-step state and diffusion record, each
+    // slice on a 256-byte boundary (vector loads).
+    static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+    size_t record_step_bytes() const {
+        const size_t n = (size_t)N;
+        return up256(n * sizeof(ushort4)) + up256(4 * n * sizeof(R)) + up256(3 * n * sizeof(R)) +
+               up256(n * sizeof(R)) + up256(record_size(n_sub, n) * sizeof(R));
+    }
+    // The arena for nsteps recorded steps (grown when needed; the graphs hold
+    // its addresses, so growing drops them).
+    bool ensure_arena(int nsteps) {
+        if (arena && arena_steps >= nsteps) return true;
+        drop_graphs();
+        if (arena) cudaFree(arena);
+        arena = nullptr;
+        arena_steps = 0;
+        rg_gid.clear(); rg_phi.clear(); rg_ph.clear(); rg_C.clear(); rg_Csub.clear();
+        const size_t per = record_step_bytes();
+        if (cudaMalloc((void **)&arena, per * (size_t)nsteps) != cudaSuccess) {
+            cudaGetLastError();
+            arena = nullptr;
+            return false;
+        }
+        const size_t n = (size_t)N;
+        for (int t = 0; t < nsteps; t++) {
+            char *b = arena + per * (size_t)t;
+            rg_gid.push_back((ushort4 *)b);
+            b += up256(n * sizeof(ushort4));
+            rg_phi.push_back((R *)b);
+            b += up256(4 * n * sizeof(R));
+            rg_ph.push_back((R *)b);
+            b += up256(3 * n * sizeof(R));
+            rg_C.push_back((R *)b);
+            b += up256(n * sizeof(R));
+            rg_Csub.push_back((R *)b);
+        }
+        arena_steps = nsteps;
+        return true;
     }
 
     ~AdjCtx() override {
@@ -719,6 +772,7 @@ struct AdjCtx : pf_adj_impl {
         f(gid0); f(phi0); f(ph0); f(C0);
         for (size_t i = 0; i < ck_gid.size(); i++) { f(ck_gid[i]); f(ck_phi[i]); f(ck_ph[i]); f(ck_C[i]); }
         for (size_t i = 0; i < sg_gid.size(); i++) { f(sg_gid[i]); f(sg_phi[i]); f(sg_ph[i]); f(sg_C[i]); f(sg_Csub[i]); }
+        f(arena);
         f(w_gid); f(w_phi); f(w_ph); f(w_C); f(w_C2); f(dscr);
         f(v_gid); f(v_phi); f(v_ph); f(v_C);
         f(l_phi); f(l_ph); f(l_C); f(l_phi2); f(l_ph2); f(l_C2); f(pub_id); f(pub_l); f(d_acc);
@@ -832,7 +886,8 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
     auto *c = new AdjCtx<R>();
     c->model = *m;
     c->N = (long long)m->ix * m->iy * m->iz;
-    c->K = K;
+    c->record = K == 0;
+    c->K = K == 0 ? 1 : K;
     const size_t N = (size_t)c->N;
     bool ok = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && c->alloc(&c->gid0, N) && c->alloc(&c->phi0, 4 * N) && c->alloc(&c->ph0, 3 * N) && c->alloc(&c->C0, N);
@@ -866,7 +921,7 @@ static int adj_create(const pf_model *m, int K, pf_adj_impl **out) {
 }
 
 extern "C" int pf_adj_create(const pf_model *model, int precision, int checkpoint_every, pf_adj **out) {
-    if (!model || !out || checkpoint_every < 1) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad arguments");
+    if (!model || !out || checkpoint_every < 0) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad arguments");
     if (precision != PF_PREC_FP64 && precision != PF_PREC_FP32C) return pf_fail(PF_ERR_ARG, "pf_adj_create: bad precision");
     if (model->thermo_model != 0)
         return pf_fail(PF_ERR_ARG, "pf_adj_create: the adjoint differentiates the linear-line thermodynamics only");
@@ -985,9 +1040,80 @@ static void copy_state(AdjCtx<R> *c, const ushort4 *g, const R *p, const R *h, c
     cudaMemcpyAsync(C2, C, N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
 }
 
+// The objective sums of the final state (ph, C) into J, with the forward's timing.
+template <typename R>
+static int adj_finish_forward(AdjCtx<R> *c, R *ph, R *C, cudaEvent_t e0, cudaEvent_t e1, double J[2]) {
+    cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
+    AP<R> P = c->P;
+    c->fin_ph = ph;
+    c->fin_C = C;
+    k_objective_sums<R><<<256, 256, 0, c->s>>>(P, ph, C, c->d_acc);
+    double h[8];
+    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaEventRecord(e1, c->s);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_forward failed");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    c->ms_fwd = ms;
+    c->J[0] = h[0] / (double)c->N;
+    c->W = h[1];
+    c->J[1] = h[1] > 0 ? h[2] / h[1] : 0.0;
+    J[0] = c->J[0];
+    J[1] = c->J[1];
+    c->have_fwd = true;
+    return PF_OK;
+}
+
+// Record mode: the forward writes every step's pre-step state and diffusion
+// record into the arena (the work a checkpointed gradient spends recomputing
+// segments), as one captured graph per step count.
+template <typename R>
+static int adj_forward_record(AdjCtx<R> *c, int nsteps, double J[2]) {
+    c->params();
+    c->nsteps = nsteps;
+    if (std::memcmp(&c->gP, &c->P, sizeof(c->P)) != 0) {
+        c->drop_graphs();
+        c->gP = c->P;
+    }
+    if (!c->ensure_arena(nsteps))
+        return pf_fail(PF_ERR_NOMEM, "pf_adj_forward: the record of every step does not fit on the device "
+                                     "(use a checkpoint interval)");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->s);
+    auto run = [&]() -> int {
+        copy_state(c, c->gid0, c->phi0, c->ph0, c->C0, c->rg_gid[0], c->rg_phi[0], c->rg_ph[0], c->rg_C[0]);
+        for (int t = 0; t < nsteps; t++) {
+            const bool last = t + 1 == nsteps;
+            const int s2 = c->step(c->rg_gid[t], c->rg_phi[t], c->rg_ph[t], c->rg_C[t],
+                                   last ? c->w_gid : c->rg_gid[t + 1], last ? c->w_phi : c->rg_phi[t + 1],
+                                   last ? c->w_ph : c->rg_ph[t + 1], last ? c->w_C : c->rg_C[t + 1], c->rg_Csub[t]);
+            if (s2 != PF_OK) return s2;
+        }
+        return PF_OK;
+    };
+    if (!c->rec_fwd || c->rec_fwd_steps != nsteps) {
+        if (c->rec_fwd) { cudaGraphExecDestroy(c->rec_fwd); c->rec_fwd = nullptr; }
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+        const int st = run();
+        if (cudaStreamEndCapture(c->s, &g) != cudaSuccess || st != PF_OK)
+            return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+        const bool okg = cudaGraphInstantiate(&c->rec_fwd, g, 0) == cudaSuccess;
+        cudaGraphDestroy(g);
+        if (!okg) return pf_fail(PF_ERR_CUDA, "adjoint: graph instantiation failed");
+        c->rec_fwd_steps = nsteps;
+    }
+    if (cudaGraphLaunch(c->rec_fwd, c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
+    return adj_finish_forward(c, c->w_ph, c->w_C, e0, e1, J);
+}
+
 template <typename R>
 static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
     if (!c->have_state) return pf_fail(PF_ERR_ARG, "pf_adj_forward: no state uploaded");
+    if (c->record) return adj_forward_record(c, nsteps, J);
     c->params();
     c->nsteps = nsteps;
     const int nck = (nsteps + c->K - 1) / c->K + 1;
@@ -1044,26 +1170,7 @@ static int adj_forward(AdjCtx<R> *c, int nsteps, double J[2]) {
         }
         if (st != PF_OK) return st;
     }
-    cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
-    AP<R> P = c->P;
-    c->fin_ph = ha;
-    c->fin_C = Ca;
-    k_objective_sums<R><<<256, 256, 0, c->s>>>(P, ha, Ca, c->d_acc);
-    double h[8];
-    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
-    cudaEventRecord(e1, c->s);
-    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_forward failed");
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0); cudaEventDestroy(e1);
-    c->ms_fwd = ms;
-    c->J[0] = h[0] / (double)c->N;
-    c->W = h[1];
-    c->J[1] = h[1] > 0 ? h[2] / h[1] : 0.0;
-    J[0] = c->J[0];
-    J[1] = c->J[1];
-    c->have_fwd = true;
-    return PF_OK;
+    return adj_finish_forward(c, ha, Ca, e0, e1, J);
 }
 
 extern "C" int pf_adj_forward(pf_adj *a, int nsteps, double J[2]) {
@@ -1071,9 +1178,101 @@ extern "C" int pf_adj_forward(pf_adj *a, int nsteps, double J[2]) {
     return a->prec == PF_PREC_FP64 ? adj_forward(as<double>(a), nsteps, J) : adj_forward(as<float>(a), nsteps, J);
 }
 
+// The gradient sums, the barrier-timeout flag and the gradient's timing.
+template <typename R>
+static int adj_finish_gradient(AdjCtx<R> *c, cudaEvent_t e0, cudaEvent_t e1, double grad[4]) {
+    double h[8];
+    int herr = 0;
+    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->s);
+    cudaEventRecord(e1, c->s);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_gradient failed");
+    if (herr) {
+        cudaMemsetAsync(c->d_err, 0, sizeof(int), c->s);
+        cudaStreamSynchronize(c->s);
+        return pf_fail(PF_ERR_TIMEOUT, "pf_adj_gradient: a grid barrier of the reverse diffusion timed out");
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    c->ms_bwd = ms;
+    grad[0] = h[3];
+    grad[1] = h[4];
+    grad[2] = h[5];
+    grad[3] = 0.0;  // Mn does not enter the phase update or the carbon field
+    return PF_OK;
+}
+
+// Record mode: seed from the final state and sweep every recorded step
+// backwards, as one captured graph per step count that ends with the adjoint
+// buffers back in the roles it was captured with.
+template <typename R>
+static int adj_gradient_record(AdjCtx<R> *c, int obj, double grad[4]) {
+    const int T = c->nsteps;
+    const size_t N = (size_t)c->N;
+    AP<R> P = c->P;
+    const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->s);
+    cudaMemsetAsync(c->d_acc, 0, 8 * sizeof(double), c->s);
+    k_seed<R><<<blocks(c->N), 256, 0, c->s>>>(P, obj, c->w_ph, c->w_C, c->W, c->J[1], c->l_ph, c->l_C, c->l_phi);
+    auto reverse = [&]() {
+        const ushort4 *pend_gid = nullptr;
+        R *pend_lphi = nullptr;
+        for (int t = T - 1; t >= 0; t--) {
+            bwd_diffusion(c, P, c->rg_Csub[t], c->rg_C[t], pend_gid, pend_lphi);
+            k_bwd_phase_own<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->rg_gid[t], c->rg_phi[t], c->rg_ph[t],
+                                                                 c->rg_C[t], c->l_phi, c->l_ph, c->l_C, c->l_phi2,
+                                                                 c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
+            pend_gid = c->rg_gid[t];
+            pend_lphi = c->l_phi2;
+            std::swap(c->l_phi, c->l_phi2);
+            std::swap(c->l_ph, c->l_ph2);
+        }
+        if (pend_gid)
+            k_bwd_phase_gather<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, pend_gid, c->pub_id, c->pub_l, pend_lphi);
+    };
+    // Move the seeded adjoint into the buffers the graph starts from.
+    auto to_roles = [&](R *gC, R *gphi, R *gph) {
+        if (c->l_C != gC) {
+            cudaMemcpyAsync(gC, c->l_C, N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+            std::swap(c->l_C, c->l_C2);
+        }
+        if (c->l_phi != gphi) {
+            cudaMemcpyAsync(gphi, c->l_phi, 4 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+            std::swap(c->l_phi, c->l_phi2);
+        }
+        if (c->l_ph != gph) {
+            cudaMemcpyAsync(gph, c->l_ph, 3 * N * sizeof(R), cudaMemcpyDeviceToDevice, c->s);
+            std::swap(c->l_ph, c->l_ph2);
+        }
+    };
+    if (!c->rec_bwd || c->rec_bwd_steps != T) {
+        if (c->rec_bwd) { cudaGraphExecDestroy(c->rec_bwd); c->rec_bwd = nullptr; }
+        R *cC = c->l_C, *cphi = c->l_phi, *cph = c->l_ph;
+        c->rb_C = cC; c->rb_phi = cphi; c->rb_ph = cph;
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+        reverse();
+        to_roles(cC, cphi, cph);
+        if (cudaStreamEndCapture(c->s, &g) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: capture failed");
+        const bool okg = cudaGraphInstantiate(&c->rec_bwd, g, 0) == cudaSuccess;
+        cudaGraphDestroy(g);
+        if (!okg) return pf_fail(PF_ERR_CUDA, "adjoint: graph instantiation failed");
+        c->rec_bwd_steps = T;
+    } else {
+        to_roles(c->rb_C, c->rb_phi, c->rb_ph);
+    }
+    if (cudaGraphLaunch(c->rec_bwd, c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
+    return adj_finish_gradient(c, e0, e1, grad);
+}
+
 template <typename R>
 static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     if (!c->have_fwd) return pf_fail(PF_ERR_ARG, "pf_adj_gradient: run pf_adj_forward first");
+    if (c->record) return adj_gradient_record(c, obj, grad);
     const int nck = (c->nsteps + c->K - 1) / c->K + 1;
     int st = ensure_ck(c, (size_t)nck, (size_t)c->K);
     if (st != PF_OK) return st;
@@ -1182,26 +1381,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
         }
         if (cudaGraphLaunch(c->seg_graph, c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "adjoint: graph launch failed");
     }
-    double h[8];
-    int herr = 0;
-    cudaMemcpyAsync(h, c->d_acc, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s);
-    cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->s);
-    cudaEventRecord(e1, c->s);
-    if (cudaStreamSynchronize(c->s) != cudaSuccess) return pf_fail(PF_ERR_CUDA, "pf_adj_gradient failed");
-    if (herr) {
-        cudaMemsetAsync(c->d_err, 0, sizeof(int), c->s);
-        cudaStreamSynchronize(c->s);
-        return pf_fail(PF_ERR_TIMEOUT, "pf_adj_gradient: a grid barrier of the reverse diffusion timed out");
-    }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0); cudaEventDestroy(e1);
-    c->ms_bwd = ms;
-    grad[0] = h[3];
-    grad[1] = h[4];
-    grad[2] = h[5];
-    grad[3] = 0.0;  // Mn does not enter the phase update or the carbon field
-    return PF_OK;
+    return adj_finish_gradient(c, e0, e1, grad);
 }
 
 extern "C" int pf_adj_gradient(pf_adj *a, int objective, double grad[4]) {

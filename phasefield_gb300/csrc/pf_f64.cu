@@ -162,6 +162,9 @@ __device__ __forceinline__ bool pf_coh_has(const int *coh, int n_coh, int aus, i
 // cell's own (k_avg_conc_f64), when P.avg_conc is set.  flags, coh (null
 // unless P.coh_model): the scan's Has_ferrite / Rex_intf bits and the
 // coherent-partner table of the Fortran model's coherent-grain mobility.
+// EXT: compiled with the solute drag and the coherent mobility (the plain
+// model's instance carries neither, and keeps its register budget).
+template <bool EXT>
 __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P,
                                                    const int *__restrict__ ids1,
                                                    const double *__restrict__ phi1,
@@ -283,7 +286,7 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
     // saw bulk ferrite and no recrystallisation front, and exactly one of the
     // cell's own grains above the cutoff (Ind_ph1(1:N_nonzero)) is ferrite.
     bool coh_cell = false;
-    if (P.coh_model && flags && coh) {
+    if (EXT && P.coh_model && flags && coh) {
         const int fl = flags[n];
         int nown = 0, nfer = 0;
 #pragma unroll
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                         const double mob = cp ? 0.02 * P.m[e] : P.m[e];
                         d = cp ? mob * d : d * mob;
                         del[ii] += d;
-                        if (P.drag_model && pi + pj == 3) drag[ii] += mob * (factor3 * sqrt(s1[ii] * s1[jj]));
+                        if (EXT && P.drag_model && pi + pj == 3) drag[ii] += mob * (factor3 * sqrt(s1[ii] * s1[jj]));
                     }
                 }
             }
@@ -332,43 +335,43 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
     // each of the cell's own grains moves at the rate that balances its
     // driving rate against the drag; a two-entry stencil keeps the second
     // rate the negative of the first.
-    if (P.drag_model) {
+    if (EXT && P.drag_model) {
         const double f = phase[3 * n], a = phase[3 * n + 1], c = phase[3 * n + 2];
         const bool co1 = f > cutoff && c > cutoff, co2 = f > cutoff && a > cutoff;
         int nown = 0;
 #pragma unroll
         for (int a6 = 0; a6 < 6; a6++) nown += own_v[a6] > cutoff ? 1 : 0;
         int fail = 0;
-        for (int ii = 0; ii < num; ii++) {
+        // With two entries only the first is solved; the second takes its
+        // negative.  Entries are picked by static index so the stencil arrays
+        // stay in registers.
+        const int nsolve = num == 2 ? 1 : num;
+        for (int ii = 0; ii < nsolve; ii++) {
             if (!co1 && co2 && ii < nown) {
-                const double drv = del[ii];
-                const double norm = factor3 * sqrt(s1[ii] * (1. - s1[ii]));
+                double drv = 0., dg = 0., v1 = 0.;
+                int ph_ii = 0;
+#pragma unroll
+                for (int t = 0; t < PF_NSTENCIL; t++)
+                    if (t == ii) {
+                        drv = del[t]; dg = drag[t]; v1 = s1[t]; ph_ii = sph[t];
+                    }
+                const double norm = factor3 * sqrt(v1 * (1. - v1));
+                // growth (austenite up, ferrite down) uses the heating branch
+                const bool active = (drv > 0. && (ph_ii == 1 || ph_ii == 2)) || (drv < 0. && (ph_ii == 1 || ph_ii == 2));
+                const bool heat = (drv > 0.) ? (ph_ii == 2) : (ph_ii == 1);
                 double r = drv;
-                if (drv > 0.) {
-                    if (sph[ii] == 2)
-                        r = pf_drag_solve(drv, drag[ii], norm, 1, drv, P.drag_vmax, P.drag_ex0, P.drag_de_heat,
-                                          P.drag_u0, P.drag_corr[0], P.drag_drag0[0], P.T, &fail);
-                    else if (sph[ii] == 1)
-                        r = pf_drag_solve(drv, drag[ii], norm, 0, drv, P.drag_vmax, P.drag_ex0, P.drag_de_cool,
-                                          P.drag_u0, P.drag_corr[1], P.drag_drag0[1], P.T, &fail);
-                } else if (drv < 0.) {
-                    if (sph[ii] == 1)
-                        r = pf_drag_solve(-drv, drag[ii], norm, 1, drv, P.drag_vmax, P.drag_ex0, P.drag_de_heat,
-                                          P.drag_u0, P.drag_corr[0], P.drag_drag0[0], P.T, &fail);
-                    else if (sph[ii] == 2)
-                        r = pf_drag_solve(-drv, drag[ii], norm, 0, drv, P.drag_vmax, P.drag_ex0, P.drag_de_cool,
-                                          P.drag_u0, P.drag_corr[1], P.drag_drag0[1], P.T, &fail);
-                    r = -r;
-                } else {
-                    r = 0.;
-                }
-                del[ii] = r;
-            }
-            if (num == 2) {
-                del[1] = -del[0];
-                break;
+                if (active)
+                    r = pf_drag_solve(drv > 0. ? drv : -drv, dg, norm, heat ? 1 : 0, drv, P.drag_vmax, P.drag_ex0,
+                                      heat ? P.drag_de_heat : P.drag_de_cool, P.drag_u0,
+                                      P.drag_corr[heat ? 0 : 1], P.drag_drag0[heat ? 0 : 1], P.T, &fail);
+                if (drv < 0.) r = -r;
+                else if (!(drv > 0.)) r = 0.;
+#pragma unroll
+                for (int t = 0; t < PF_NSTENCIL; t++)
+                    if (t == ii) del[t] = r;
             }
         }
+        if (num == 2) del[1] = -del[0];
         if (fail) atomicExch(&g_drag_fail, 1);
     }
 #pragma unroll
@@ -528,9 +531,13 @@ cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const 
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    k_phase_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(
-        P, ids1, phi1, ids2, phi2, phase, conc1, C, scanned ? avg : nullptr, coherent ? flags : nullptr,
-        coherent ? coh : nullptr, n_coh);
+    if (P.drag_model || coherent)
+        k_phase_f64<true><<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(
+            P, ids1, phi1, ids2, phi2, phase, conc1, C, scanned ? avg : nullptr, coherent ? flags : nullptr,
+            coherent ? coh : nullptr, n_coh);
+    else
+        k_phase_f64<false><<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(
+            P, ids1, phi1, ids2, phi2, phase, conc1, C, scanned ? avg : nullptr, nullptr, nullptr, 0);
     return cudaGetLastError();
 }
 

@@ -52,14 +52,54 @@ def test_adjoint_matches_central_differences(gpu, tmp_path, obj):
 
 
 def test_gradient_independent_of_checkpoint_interval(gpu, tmp_path):
+    """Checkpoint intervals 3, 4 and 50 and the record mode (0: every step
+    kept by the forward, no recomputation) give the same objective and
+    gradient; in record mode a repeated forward/gradient (graph replays)
+    gives them again."""
     steps = 15
-    out = []
-    for K in (3, 4, 50):
+    out, Js = [], []
+    for K in (3, 4, 50, 0):
         A = _setup(tmp_path, K=K)
-        A.forward(steps)
+        Js.append(A.forward(steps))
         out.append(A.gradient(1))
+        if K == 0:
+            # J sums per-block FP64 partials with atomics: equal to rounding
+            np.testing.assert_allclose(A.forward(steps), Js[-1], rtol=1e-13)
+            np.testing.assert_allclose(A.gradient(1), out[-1], rtol=1e-12, atol=1e-300)
+            A.gradient(0)
+            np.testing.assert_allclose(A.gradient(1), out[-1], rtol=1e-12, atol=1e-300)
+        A.close()
+    for J in Js[1:]:
+        np.testing.assert_allclose(J, Js[0], rtol=1e-13)
     for g in out[1:]:
         np.testing.assert_allclose(g, out[0], rtol=1e-10, atol=1e-300)
+
+
+def test_record_mode_matches_central_differences(gpu, tmp_path):
+    """Record mode against central differences of the FP64 forward (the
+    checkpointed gradient's tolerance)."""
+    steps = 20
+    A = _setup(tmp_path, K=0)
+    A.forward(steps)
+    g = A.gradient(0)
+    fd = [_fd(A, steps, 0, i) for i in range(3)]
+    for i in range(3):
+        scale = max(abs(fd[i]), 1e-3 * max(abs(x) for x in fd))
+        assert abs(g[i] - fd[i]) <= 2e-3 * scale, (i, g[i], fd[i])
+
+
+def test_record_mode_fp32_equals_checkpointed(gpu, tmp_path):
+    """FP32 calibration: record mode and checkpoint interval 7 agree."""
+    steps = 30
+    res = []
+    for K in (7, 0):
+        A = _setup(tmp_path, prec=pf.PF_PREC_FP32C, K=K)
+        J = A.forward(steps)
+        res.append((J, A.gradient(0), A.gradient(1)))
+        A.close()
+    np.testing.assert_allclose(res[1][0], res[0][0], rtol=1e-12)
+    np.testing.assert_allclose(res[1][1], res[0][1], rtol=1e-9, atol=1e-300)
+    np.testing.assert_allclose(res[1][2], res[0][2], rtol=1e-9, atol=1e-300)
 
 
 def test_torch_autograd_wrapper(gpu, tmp_path):
