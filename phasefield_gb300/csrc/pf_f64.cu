@@ -446,14 +446,45 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
     }
 }
 
+// Flux weights of the forward links of every cell (solver.cpp:363):
+// links[9n + 3d + p] = sqrt(phase_p(n + e_d) * phase_p(n)) for d = x+, y+, z+
+// (the directions the stencil uses).  The phase fractions stay fixed through
+// a step's diffusion sub-steps, so the sub-steps read these instead of taking
+// 18 FP64 square roots per cell each (FP64 arithmetic is scarce on GB300).  A
+// link is shared by its two cells and a*b == b*a exactly, so both read the
+// weight the reference computes for them.
+__global__ void __launch_bounds__(256) k_links_f64(const __grid_constant__ pf_step_params P, int nnb,
+                                                   const double *__restrict__ phase,
+                                                   double *__restrict__ links) {
+    int ci, cj, ck;
+    long long n;
+    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
+    long long nbr[6];
+    pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nbr);
+    double ph[3];
+    ph[0] = __ldg(phase + 3 * n + 0);
+    ph[1] = __ldg(phase + 3 * n + 1);
+    ph[2] = __ldg(phase + 3 * n + 2);
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        if (2 * d + 1 < nnb) {
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+                links[9 * n + 3 * d + p] = sqrt(__ldg(phase + 3 * nbr[2 * d + 1] + p) * ph[p]);
+        }
+}
+
 // Diffusion_solver (solver.cpp:343-372) for every solute, one thread per cell:
 // reads phase/conc1 of the cell and its nnb neighbours, updates C in place and
-// writes the re-partitioned concentrations to conc2.  With nnb = 6 and
-// coef = dt/num_loop/dx^2 it is also one sub-step of the reference's GPU
-// plug-in (gpu_solver.cpp:131-188): the partition written here is exactly what
-// GPU_Partitioning computes at the start of the next sub-step.
+// writes the re-partitioned concentrations to conc2.  The flux weight of
+// neighbour b, sqrt(phase_p^nb * phase_p), comes from links (k_links_f64): the
+// cell's own forward link for x+, y+, z+, the neighbour's for x-, y-, z-.
+// With nnb = 6 and coef = dt/num_loop/dx^2 it is also one sub-step of the
+// reference's GPU plug-in (gpu_solver.cpp:131-188): the partition written here
+// is exactly what GPU_Partitioning computes at the start of the next sub-step.
 __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_step_params P, int nnb,
                                                      double coef, const double *__restrict__ phase,
+                                                     const double *__restrict__ links,
                                                      const double *__restrict__ conc1,
                                                      double *__restrict__ conc2,
                                                      double *__restrict__ C) {
@@ -466,14 +497,13 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
     ph[0] = __ldg(phase + 3 * n + 0);
     ph[1] = __ldg(phase + 3 * n + 1);
     ph[2] = __ldg(phase + 3 * n + 2);
-    // Flux weights sqrt(phase_p^nb * phase_p) (solver.cpp:363) do not depend on
-    // the solute: evaluated once per cell, not once per solute.
     double w[6][3];
 #pragma unroll
     for (int b = 0; b < 6; b++)
         if (b < nnb) {
+            const long long at = (b & 1) ? 9 * n + 3 * (b >> 1) : 9 * nbr[b] + 3 * (b >> 1);
 #pragma unroll
-            for (int p = 0; p < 3; p++) w[b][p] = sqrt(__ldg(phase + 3 * nbr[b] + p) * ph[p]);
+            for (int p = 0; p < 3; p++) w[b][p] = __ldg(links + at + p);
         }
     for (int q = 0; q < P.nsol; q++) {
         const double *c1 = conc1 + (long long)q * 3 * P.N;
@@ -541,9 +571,17 @@ cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const 
     return cudaGetLastError();
 }
 
+cudaError_t pf_launch_links_f64(const pf_step_params &P, int nnb, const double *phase, double *links,
+                                cudaStream_t s) {
+    k_links_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, phase, links);
+    return cudaGetLastError();
+}
+
 cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
-                                  const double *conc1, double *conc2, double *C, cudaStream_t s) {
-    k_diffuse_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, coef, phase, conc1, conc2, C);
+                                  const double *links, const double *conc1, double *conc2, double *C,
+                                  cudaStream_t s) {
+    k_diffuse_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, coef, phase, links, conc1,
+                                                                             conc2, C);
     return cudaGetLastError();
 }
 
