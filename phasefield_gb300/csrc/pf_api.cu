@@ -31,6 +31,7 @@ struct DropIn {
     int x = 0, y = 0, z = 0;
     double *phase = nullptr, *C = nullptr, *conc[2] = {nullptr, nullptr};
     double *links = nullptr;  // flux weights of the forward links (k_links_f64)
+    double *tpart = nullptr;  // partition sums of the fixed phase fractions
     bool ready = false;
 } g_drop;
 
@@ -40,6 +41,7 @@ void dropin_free() {
     cudaFree(g_drop.conc[0]);
     cudaFree(g_drop.conc[1]);
     cudaFree(g_drop.links);
+    cudaFree(g_drop.tpart);
     g_drop = DropIn();
 }
 }  // namespace
@@ -56,9 +58,10 @@ extern "C" int GPU_Init(const int x, const int y, const int z) {
     const size_t N = (size_t)x * y * z;
     size_t freeb = 0, total = 0;
     cudaMemGetInfo(&freeb, &total);
-    if (N * sizeof(double) * 19 > freeb) return 0;
+    if (N * sizeof(double) * 25 > freeb) return 0;
     if (cudaMalloc(&g_drop.phase, 3 * N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&g_drop.links, 9 * N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&g_drop.tpart, 6 * N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&g_drop.C, N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&g_drop.conc[0], 3 * N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&g_drop.conc[1], 3 * N * sizeof(double)) != cudaSuccess) {
@@ -101,10 +104,10 @@ extern "C" void GPU_Diffusion_solver(double *hdiffusivity, double *hpartition_k,
     cudaMemcpy(g_drop.phase, hvalue_phase, 3 * N * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(g_drop.C, htotal_conc, N * sizeof(double), cudaMemcpyHostToDevice);
     pf_launch_partition_f64(P, g_drop.phase, g_drop.C, g_drop.conc[0], s);
-    pf_launch_links_f64(P, 6, g_drop.phase, g_drop.links, s);  // phases fixed for the whole call
+    pf_launch_links_f64(P, 6, g_drop.phase, g_drop.links, g_drop.tpart, s);  // phases fixed for the whole call
     int a = 0;
     for (int it = 1; it <= num_loop; it++) {
-        pf_launch_diffuse_f64(P, 6, dt_dxdx, g_drop.phase, g_drop.links, g_drop.conc[a], g_drop.conc[1 - a],
+        pf_launch_diffuse_f64(P, 6, dt_dxdx, g_drop.links, g_drop.tpart, g_drop.conc[a], g_drop.conc[1 - a],
                               g_drop.C, s);
         a = 1 - a;
     }
@@ -136,6 +139,7 @@ struct pf_ctx {
     double *C = nullptr;
     double *avg = nullptr;  // interface-averaged concentrations (models with avg_carbon or coherent)
     double *links = nullptr;  // flux weights of the forward links, refreshed after each phase sweep
+    double *tpart = nullptr;  // partition sums of the same phase fractions
     unsigned char *coh_flags = nullptr;  // Has_ferrite / Rex_intf per cell (models with coherent)
     int *coh = nullptr;                  // coherent partners, 2 per austenite grain
     int n_coh = 0;
@@ -233,7 +237,7 @@ void free_all(pf_ctx *c) {
         cudaFree(c->ids[i]); cudaFree(c->phi[i]); cudaFree(c->conc[i]);
         cudaFree(c->gid[i]); cudaFree(c->phi32[i]); cudaFree(c->sol[i]);
     }
-    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->avg); cudaFree(c->links); cudaFree(c->coh_flags); cudaFree(c->coh); cudaFree(c->phase32);
+    cudaFree(c->phase); cudaFree(c->C); cudaFree(c->avg); cudaFree(c->links); cudaFree(c->tpart); cudaFree(c->coh_flags); cudaFree(c->coh); cudaFree(c->phase32);
     cudaFree(c->d_span); cudaFree(c->d_trunc); cudaFree(c->rest); cudaFree(c->rest_count);
     cudaFree(c->st_ids); cudaFree(c->st_phi); cudaFree(c->st_phase); cudaFree(c->st_C); cudaFree(c->st_conc);
     cudaFree(c->partials); cudaFree(c->d_red);
@@ -257,12 +261,12 @@ cudaError_t launch_step(pf_ctx *c, const pf_step_params &P) {
         });
         if (e != cudaSuccess) return e;
         c->cur = 1 - a;
-        e = timed(c, 1, [&] { return pf_launch_links_f64(P, P.nnb, c->phase, c->links, c->stream); });
+        e = timed(c, 1, [&] { return pf_launch_links_f64(P, P.nnb, c->phase, c->links, c->tpart, c->stream); });
         if (e != cudaSuccess) return e;
         for (int it = 0; it < P.n_sub; it++) {
             const int b = c->curc;
             e = timed(c, 1, [&] {
-                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->phase, c->links, c->conc[b], c->conc[1 - b],
+                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->links, c->tpart, c->conc[b], c->conc[1 - b],
                                              c->C, c->stream);
             });
             if (e != cudaSuccess) return e;
@@ -393,6 +397,7 @@ extern "C" int pf_create(const pf_model *model, int precision, pf_ctx **out) {
         }
         alloc((void **)&c->phase, 3 * N * sizeof(double));
         alloc((void **)&c->links, 9 * N * sizeof(double));
+        alloc((void **)&c->tpart, 6 * N * c->nsol * sizeof(double));
         alloc((void **)&c->C, N * c->nsol * sizeof(double));
         if (model->avg_carbon || model->coherent) alloc((void **)&c->avg, 3 * N * sizeof(double));
         if (model->coherent) alloc((void **)&c->coh_flags, N);
@@ -596,11 +601,11 @@ extern "C" int pf_diffuse(pf_ctx *c, int nsub) {
     pf_compute_params(c->model, c->time, P);
     cudaError_t e = cudaSuccess;
     if (c->prec == PF_PREC_FP64) {
-        if (nsub > 0) e = pf_launch_links_f64(P, P.nnb, c->phase, c->links, c->stream);
+        if (nsub > 0) e = pf_launch_links_f64(P, P.nnb, c->phase, c->links, c->tpart, c->stream);
         for (int it = 0; it < nsub && e == cudaSuccess; it++) {
             const int b = c->curc;
             e = timed(c, 1, [&] {
-                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->phase, c->links, c->conc[b], c->conc[1 - b],
+                return pf_launch_diffuse_f64(P, P.nnb, P.coef_diff, c->links, c->tpart, c->conc[b], c->conc[1 - b],
                                              c->C, c->stream);
             });
             c->curc = 1 - b;

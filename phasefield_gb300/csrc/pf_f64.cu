@@ -453,9 +453,12 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
 // 18 FP64 square roots per cell each (FP64 arithmetic is scarce on GB300).  A
 // link is shared by its two cells and a*b == b*a exactly, so both read the
 // weight the reference computes for them.
+// tpart[6(qN + n) + i], tpart[6(qN + n) + 3 + i]: the sums t1_i, t2_i of the
+// partition (solver.cpp:389-405) of solute q, also fixed through the
+// sub-steps; a sub-step then only divides, (C - t2_i) / t1_i.
 __global__ void __launch_bounds__(256) k_links_f64(const __grid_constant__ pf_step_params P, int nnb,
                                                    const double *__restrict__ phase,
-                                                   double *__restrict__ links) {
+                                                   double *__restrict__ links, double *__restrict__ tpart) {
     int ci, cj, ck;
     long long n;
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
@@ -472,19 +475,34 @@ __global__ void __launch_bounds__(256) k_links_f64(const __grid_constant__ pf_st
             for (int p = 0; p < 3; p++)
                 links[9 * n + 3 * d + p] = sqrt(__ldg(phase + 3 * nbr[2 * d + 1] + p) * ph[p]);
         }
+    for (int q = 0; q < P.nsol; q++) {
+        double *tp = tpart + 6 * ((long long)q * P.N + n);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            double t1 = 0., t2 = 0.;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                t1 += ph[j] * P.k[q][i + 3 * j];
+                t2 += ph[j] * P.c[q][i + 3 * j];
+            }
+            tp[i] = t1;
+            tp[3 + i] = t2;
+        }
+    }
 }
 
 // Diffusion_solver (solver.cpp:343-372) for every solute, one thread per cell:
 // reads phase/conc1 of the cell and its nnb neighbours, updates C in place and
 // writes the re-partitioned concentrations to conc2.  The flux weight of
 // neighbour b, sqrt(phase_p^nb * phase_p), comes from links (k_links_f64): the
-// cell's own forward link for x+, y+, z+, the neighbour's for x-, y-, z-.
+// cell's own forward link for x+, y+, z+, the neighbour's for x-, y-, z-;
+// the partition's sums come from tpart (same arithmetic, done once per step).
 // With nnb = 6 and coef = dt/num_loop/dx^2 it is also one sub-step of the
 // reference's GPU plug-in (gpu_solver.cpp:131-188): the partition written here
 // is exactly what GPU_Partitioning computes at the start of the next sub-step.
 __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_step_params P, int nnb,
-                                                     double coef, const double *__restrict__ phase,
-                                                     const double *__restrict__ links,
+                                                     double coef, const double *__restrict__ links,
+                                                     const double *__restrict__ tpart,
                                                      const double *__restrict__ conc1,
                                                      double *__restrict__ conc2,
                                                      double *__restrict__ C) {
@@ -493,10 +511,6 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
     if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
     long long nbr[6];
     pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nbr);
-    double ph[3];
-    ph[0] = __ldg(phase + 3 * n + 0);
-    ph[1] = __ldg(phase + 3 * n + 1);
-    ph[2] = __ldg(phase + 3 * n + 2);
     double w[6][3];
 #pragma unroll
     for (int b = 0; b < 6; b++)
@@ -522,10 +536,10 @@ __global__ void __launch_bounds__(256) k_diffuse_f64(const __grid_constant__ pf_
         del *= coef;
         const double cn = C[q * P.N + n] + del;
         C[q * P.N + n] = cn;
-        double out[3];
-        pf_partition(cn, ph, P.k[q], P.c[q], out);
+        const double *tp = tpart + 6 * ((long long)q * P.N + n);
         double *cp = conc2 + (long long)q * 3 * P.N + 3 * n;
-        cp[0] = out[0]; cp[1] = out[1]; cp[2] = out[2];
+#pragma unroll
+        for (int i = 0; i < 3; i++) cp[i] = (cn - __ldg(tp + 3 + i)) / __ldg(tp + i);
     }
 }
 
@@ -572,15 +586,15 @@ cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const 
 }
 
 cudaError_t pf_launch_links_f64(const pf_step_params &P, int nnb, const double *phase, double *links,
-                                cudaStream_t s) {
-    k_links_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, phase, links);
+                                double *tpart, cudaStream_t s) {
+    k_links_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, phase, links, tpart);
     return cudaGetLastError();
 }
 
-cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
-                                  const double *links, const double *conc1, double *conc2, double *C,
+cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *links,
+                                  const double *tpart, const double *conc1, double *conc2, double *C,
                                   cudaStream_t s) {
-    k_diffuse_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, coef, phase, links, conc1,
+    k_diffuse_f64<<<pf_cell_grid(P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, nnb, coef, links, tpart, conc1,
                                                                              conc2, C);
     return cudaGetLastError();
 }

@@ -14,12 +14,13 @@ cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const 
 // 1 if a solute-drag velocity iteration of the FP64 sweep found no root since
 // the last call (then cleared).
 int pf_drag_take_failure();
-// links: 9N doubles, the flux weights of every cell's forward links, valid
-// while the phase fractions are unchanged (pf_launch_links_f64).
+// links: 9N doubles, the flux weights of every cell's forward links; tpart:
+// 6N doubles per solute, the partition sums; both valid while the phase
+// fractions are unchanged (pf_launch_links_f64).
 cudaError_t pf_launch_links_f64(const pf_step_params &P, int nnb, const double *phase, double *links,
-                                cudaStream_t s);
-cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *phase,
-                                  const double *links, const double *conc1, double *conc2, double *C,
+                                double *tpart, cudaStream_t s);
+cudaError_t pf_launch_diffuse_f64(const pf_step_params &P, int nnb, double coef, const double *links,
+                                  const double *tpart, const double *conc1, double *conc2, double *C,
                                   cudaStream_t s);
 cudaError_t pf_launch_partition_f64(const pf_step_params &P, const double *phase, const double *C,
                                     double *conc, cudaStream_t s);
