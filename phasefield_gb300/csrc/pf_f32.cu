@@ -16,7 +16,13 @@
 namespace {
 
 constexpr int kPX = 32, kPY = 8, kPT = kPX * kPY;  // phase-sweep block: 32 x 8 cells of one plane
-static_assert(kPX == 32, "one warp per tile row");
+// Each warp takes a compact patch (not a 32-cell row): a compact patch is
+// more often all bulk or all interface, so fewer lanes idle while others run
+// the list update.  2D: 8 x 4 patches of a 32 x 8 block.  3D (Z2): 4 x 4 x 2
+// patches of a 16 x 8 x 2 block.
+constexpr int kWX = 8, kWY = 4;
+static_assert(kPX % kWX == 0 && kPY % kWY == 0 && kWX * kWY == 32, "warp patches tile the block");
+constexpr int kZX = 16, kZY = 8;  // Z2 block: 16 x 8 cells on each of two planes
 
 // Phase sweep, one thread per cell, 2D blocks of 32x8 cells of one plane (x-y
 // neighbours mostly in the same block's L1 footprint).  Every cell whose
@@ -38,7 +44,7 @@ __device__ __forceinline__ void pf_defer(bool defer, unsigned n, unsigned int *r
 
 // Four resident blocks per SM (64 registers): measured faster than three
 // (75 registers, no spills) or five and six (heavy spills).
-template <int NSOL, int MINB>
+template <int NSOL, int MINB, bool Z2>
 __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__ pf_f32_params P,
                                                          const ushort4 *__restrict__ gid1,
                                                          const float4 *__restrict__ phi1,
@@ -48,16 +54,24 @@ __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__
                                                          unsigned int *__restrict__ rest,
                                                          unsigned int *__restrict__ rest_count) {
     const int ix = P.ix, iy = P.iy, iz = P.iz;
-    const int i = blockIdx.x * kPX + threadIdx.x;
-    const int j = blockIdx.y * kPY + threadIdx.y;
-    const int k = blockIdx.z;
+    const int warp = threadIdx.y, lane = threadIdx.x;  // blockDim = (32, 8): one warp per y index
+    int i, j, k;
+    if (Z2) {
+        i = blockIdx.x * kZX + (warp % (kZX / 4)) * 4 + (lane & 3);
+        j = blockIdx.y * kZY + (warp / (kZX / 4)) * 4 + ((lane >> 2) & 3);
+        k = 2 * blockIdx.z + (lane >> 4);
+    } else {
+        i = blockIdx.x * kPX + (warp % (kPX / kWX)) * kWX + lane % kWX;
+        j = blockIdx.y * kPY + (warp / (kPX / kWX)) * kWY + lane / kWX;
+        k = blockIdx.z;
+    }
     __shared__ float4 coef[9];
     pf_coef_table(P, coef);
     __syncthreads();
     const unsigned plane = (unsigned)ix * (unsigned)iy;
     const unsigned n = (unsigned)i + (unsigned)ix * (unsigned)j + plane * (unsigned)k;
     bool defer = false;
-    if (i < ix && j < iy) {
+    if (i < ix && j < iy && k < iz) {
         unsigned nb[6];
         nb[0] = n - i + pf_wrap(i, ix, -1);
         nb[1] = n - i + pf_wrap(i, ix, 1);
@@ -67,7 +81,7 @@ __global__ void __launch_bounds__(kPT, MINB) k_phase_f32(const __grid_constant__
         nb[5] = n + plane * (pf_wrap(k, iz, 1) - k);
         defer = !pf_phase_cell_reg<NSOL>(P, coef, n, nb, gid1, phi1, gid2, phi2, sphase, sol);
     }
-    // One row of the block is one warp: every lane reaches the vote.
+    // Every lane of the warp reaches the vote.
     pf_defer(defer, n, rest, rest_count);
 }
 
@@ -315,17 +329,22 @@ cudaError_t pf_launch_phase_f32(const pf_f32_params &P, const ushort4 *gid1, con
                                 ushort4 *gid2, float4 *phi2, float *sphase, const float2 *sol,
                                 unsigned int *rest, unsigned int *rest_count, cudaStream_t s) {
     const dim3 block(kPX, kPY);
-    const dim3 grid((unsigned)((P.ix + kPX - 1) / kPX), (unsigned)((P.iy + kPY - 1) / kPY), (unsigned)P.iz);
+    const bool z2 = P.iz > 1;
+    const dim3 grid = z2 ? dim3((unsigned)((P.ix + kZX - 1) / kZX), (unsigned)((P.iy + kZY - 1) / kZY),
+                                (unsigned)((P.iz + 1) / 2))
+                         : dim3((unsigned)((P.ix + kPX - 1) / kPX), (unsigned)((P.iy + kPY - 1) / kPY), 1u);
     long long rb = (P.N / 32 + kPT - 1) / kPT;  // the rest kernel loops if more than 1/32 of the cells wait
     if (rb > 152 * 8) rb = 152 * 8;
     if (rb < 1) rb = 1;
     cudaError_t e = cudaMemsetAsync(rest_count, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     if (P.nsol == 2) {
-        k_phase_f32<2, 4><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        if (z2) k_phase_f32<2, 4, true><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        else k_phase_f32<2, 4, false><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
         k_phase_f32_rest<2><<<(unsigned)rb, kPT, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
     } else {
-        k_phase_f32<1, 4><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        if (z2) k_phase_f32<1, 4, true><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
+        else k_phase_f32<1, 4, false><<<grid, block, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
         k_phase_f32_rest<1><<<(unsigned)rb, kPT, 0, s>>>(P, gid1, phi1, gid2, phi2, sphase, sol, rest, rest_count);
     }
     return cudaGetLastError();
