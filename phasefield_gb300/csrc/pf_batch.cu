@@ -181,7 +181,9 @@ __global__ void __launch_bounds__(kBX * BY, 1024 / (kBX * BY)) k_batch(const pf_
         // Phase sweep of the group's tiles.
         for (int tile = lb; tile < D.tiles; tile += nb) {
             const int tx0 = (tile % D.tiles_x) * kBX, ty0 = (tile / D.tiles_x) * BY;
-            const int i = tx0 + threadIdx.x % kBX, j = ty0 + threadIdx.x / kBX;
+            // each warp takes an 8 x 4 patch of the tile (lanes more often all bulk or all interface)
+            const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const int i = tx0 + (w % (kBX / 8)) * 8 + (lane & 7), j = ty0 + (w / (kBX / 8)) * 4 + (lane >> 3);
             if (i < P.ix && j < P.iy)
                 pf_phase_cell<NSOL, kBT, true>(P, i, j, 0, threadIdx.x, D.gid[g], D.phi[g], D.gid[g ^ 1],
                                                D.phi[g ^ 1], D.sph, D.sol[sidx], sm.L);
