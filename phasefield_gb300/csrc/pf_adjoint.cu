@@ -210,11 +210,11 @@ __device__ __forceinline__ R cpart(const AP<R> &P, const R *DS, int p, long long
 // Phase sweep; also writes the step's diffusion planes (step_planes) of the
 // new phase fractions.
 template <typename R>
-__global__ void k_fwd_phase(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph, const R *C, ushort4 *gid2,
-                            R *phi2, R *ph2, R *DS) {
+__global__ void k_fwd_phase(const AP<R> P, bool patch, const ushort4 *gid, const R *phi, const R *ph, const R *C,
+                            ushort4 *gid2, R *phi2, R *ph2, R *DS) {
     int ci, cj, ck;
     long long n;
-    if (!pf_cell(P.ix, P.iy, ci, cj, ck, n)) return;
+    if (!pf_cell_map(patch, P.ix, P.iy, ci, cj, ck, n)) return;
     Lst<R> L;
     build_list(P, ci, cj, ck, n, gid, phi, C, L);
     if (L.bulk) {
@@ -502,12 +502,12 @@ __global__ void k_seed(const AP<R> P, int obj, const R *ph, const R *C, double W
 // lam_C += driving-force part, the published neighbour-sum adjoints (ids, lS),
 // grad[0..1] += dJ/ds_m, dJ/ds_sigma.
 template <typename R>
-__global__ void k_bwd_phase_own(const AP<R> P, const ushort4 *gid, const R *phi, const R *ph_pre, const R *C,
-                                const R *lphi_post, const R *lph_post, R *lC, R *lphi_pre, R *lph_pre, int *pub_id,
-                                R *pub_l, double *grad) {
+__global__ void k_bwd_phase_own(const AP<R> P, bool patch, const ushort4 *gid, const R *phi, const R *ph_pre,
+                                const R *C, const R *lphi_post, const R *lph_post, R *lC, R *lphi_pre, R *lph_pre,
+                                int *pub_id, R *pub_l, double *grad) {
     int ci, cj, ck;
     long long n;
-    const bool in = pf_cell(P.ix, P.iy, ci, cj, ck, n);
+    const bool in = pf_cell_map(patch, P.ix, P.iy, ci, cj, ck, n);
     R gm = 0, gs = 0;  // s_m dJ/ds_m and s_sigma dJ/ds_sigma of this cell
     if (in) {
         Lst<R> L;
@@ -822,7 +822,9 @@ struct AdjCtx : pf_adj_impl {
         const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
         R *DS = Drec ? Drec : dscr;
         R *Csub = Drec ? Drec + 9 * N : nullptr;
-        k_fwd_phase<R><<<g3, PF_CELL_THREADS, 0, s>>>(P, g, phi, ph, C, g2, phi2, ph2, DS);
+        const bool pt = pf_use_patch(P.iy);  // warps on 8 x 4 cell patches
+        k_fwd_phase<R><<<pf_map_grid(pt, P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, pt, g, phi, ph, C, g2, phi2,
+                                                                                   ph2, DS);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
         // one lands in C2 and no sub-step reads the buffer it writes.
         R *buf[2] = {C2, w_C2};
@@ -1212,6 +1214,8 @@ static int adj_gradient_record(AdjCtx<R> *c, int obj, double grad[4]) {
     const size_t N = (size_t)c->N;
     AP<R> P = c->P;
     const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
+    const bool pt = pf_use_patch(P.iy);  // reverse phase sweep: warps on 8 x 4 cell patches
+    const dim3 gp = pf_map_grid(pt, P.ix, P.iy, P.iz);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, c->s);
@@ -1222,7 +1226,7 @@ static int adj_gradient_record(AdjCtx<R> *c, int obj, double grad[4]) {
         R *pend_lphi = nullptr;
         for (int t = T - 1; t >= 0; t--) {
             bwd_diffusion(c, P, c->rg_Csub[t], c->rg_C[t], pend_gid, pend_lphi);
-            k_bwd_phase_own<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->rg_gid[t], c->rg_phi[t], c->rg_ph[t],
+            k_bwd_phase_own<R><<<gp, PF_CELL_THREADS, 0, c->s>>>(P, pt, c->rg_gid[t], c->rg_phi[t], c->rg_ph[t],
                                                                  c->rg_C[t], c->l_phi, c->l_ph, c->l_C, c->l_phi2,
                                                                  c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
             pend_gid = c->rg_gid[t];
@@ -1280,6 +1284,8 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     const unsigned nb = blocks(c->N);
     AP<R> P = c->P;
     const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
+    const bool pt = pf_use_patch(P.iy);  // reverse phase sweep: warps on 8 x 4 cell patches
+    const dim3 gp = pf_map_grid(pt, P.ix, P.iy, P.iz);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, c->s);
@@ -1311,7 +1317,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
             // they need of the post-sweep phase fractions).
             bwd_diffusion(c, P, c->sg_Csub[i], c->sg_C[i], pend_gid, pend_lphi);
             // Reverse the phase sweep, own part.
-            k_bwd_phase_own<R><<<g3, PF_CELL_THREADS, 0, c->s>>>(P, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
+            k_bwd_phase_own<R><<<gp, PF_CELL_THREADS, 0, c->s>>>(P, pt, c->sg_gid[i], c->sg_phi[i], c->sg_ph[i], c->sg_C[i], c->l_phi,
                                                     c->l_ph, c->l_C, c->l_phi2, c->l_ph2, c->pub_id, c->pub_l, c->d_acc + 3);
             pend_gid = c->sg_gid[i];
             pend_lphi = c->l_phi2;
