@@ -24,13 +24,27 @@ struct Part {
 __global__ void __launch_bounds__(256) k_init(const __grid_constant__ pfinit::Setup S, const __grid_constant__ Part T,
                                               long long N, int32_t *__restrict__ ids, double *__restrict__ phi,
                                               double *__restrict__ phase, double *__restrict__ conc,
-                                              double *__restrict__ C, int *__restrict__ crowded) {
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    const int i = (int)(n % S.ix);
-    const long long r = n / S.ix;
-    const int j = (int)(r % S.iy);
-    const int k = (int)(r / S.iy);
+                                              double *__restrict__ C, int *__restrict__ crowded, bool patch) {
+    // patch (grids of at least 8 rows): 32 x 8 cells of one plane per block,
+    // each warp an 8 x 4 patch, whose lanes search the same seed buckets;
+    // else consecutive cells.
+    long long n;
+    int i, j, k;
+    if (patch) {
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        i = blockIdx.x * 32 + (w & 3) * 8 + (lane & 7);
+        j = blockIdx.y * 8 + (w >> 2) * 4 + (lane >> 3);
+        k = blockIdx.z;
+        if (i >= S.ix || j >= S.iy) return;
+        n = i + (long long)S.ix * (j + (long long)S.iy * k);
+    } else {
+        n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (n >= N) return;
+        i = (int)(n % S.ix);
+        const long long r = n / S.ix;
+        j = (int)(r % S.iy);
+        k = (int)(r / S.iy);
+    }
     int32_t id[6];
     double ph6[6], ph[3], Cv[2];
     if (!pfinit::cell(S, i, j, k, id, ph6, ph, Cv)) atomicExch(crowded, 1);
@@ -97,7 +111,10 @@ int pf_init_generate_device(int ix, int iy, int iz, int nsol, double cutoff, con
                 T.c[q][a] = cq ? cq[q * 9 + a] : 0.0;
             }
         const long long N = (long long)ix * iy * iz;
-        k_init<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(S, T, N, d_ids, d_phi, d_phase, d_conc, d_C, d_crowded);
+        const bool patch = iy >= 8;
+        const dim3 grid = patch ? dim3((unsigned)((ix + 31) / 32), (unsigned)((iy + 7) / 8), (unsigned)iz)
+                                : dim3((unsigned)((N + 255) / 256));
+        k_init<<<grid, 256, 0, s>>>(S, T, N, d_ids, d_phi, d_phase, d_conc, d_C, d_crowded, patch);
         ok = cudaGetLastError() == cudaSuccess &&
              cudaMemcpyAsync(&crowded, d_crowded, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
              cudaStreamSynchronize(s) == cudaSuccess;
