@@ -24,7 +24,7 @@ host cores over the same workload and configuration, one bounded sample per
 step (a z slab of the same seeded state, generated by the oracle library's own
 copy of the input generator; the product library is not loaded).
 
-Multi-GPU (--gpus N under torchrun): one domain does not shard in this build,
+Multi-GPU (--gpus N under torchrun): one domain is not decomposed across GPUs,
 so each rank advances an independent replica (different seed);
 value = all ranks' cells x steps / max-over-ranks time ("scaling": "weak").
 """

@@ -202,7 +202,7 @@ typedef struct {
 const char *pf_status_string(int status);
 const char *pf_last_error(void);
 /* sizeof(pf_model), sizeof(pf_step_params), sizeof(pf_init_spec): lets a
- * binding check its struct mirrors against this build. */
+ * binding check its struct mirrors against the library it loaded. */
 int pf_abi_sizes(long long out[3]);
 
 /* Parse the reference configuration file and the thermodynamic file it names

@@ -1,4 +1,4 @@
-"""Build recipes for the checker side (test infrastructure only).
+"""Build recipes for the oracle side (test infrastructure only).
 
 * ``build_oracle()`` compiles the FP64 CPU oracle ``pf_oracle.c`` into
   ``oracle/_build/liboracle.so`` with ``-ffp-contract=off`` (no fused

@@ -1,9 +1,13 @@
 /*
  * pf_oracle.c -- FP64 CPU oracle of the Steinbach multi-phase-field step.
  *
- * TEST INFRASTRUCTURE ONLY (the checker; never linked into the product).
- * Parity unpinned for the phase sweep: the reference has no tests or golden
- * outputs and cannot be built here (Blitz++ missing).  Every function cites
+ * TEST INFRASTRUCTURE ONLY (the oracle; never linked into the product).
+ * Pinned: tests/test_golden.py checks it bit for bit against full time steps
+ * of the reference's own CPU code (built unmodified against the minimal
+ * Blitz++ stand-in of oracle/blitz_shim; tests/golden/ref_cpu_steps.npz) and
+ * against the reference's CUDA diffusion kernels (ref_gpu_diffusion.npz); the
+ * Fortran-model options are checked against literal restatements of the
+ * Fortran loops in the tests (no Fortran compiler here).  Every function cites
  * the reference file:line (paths inside zhubq/PhaseField) it restates.  The
  * arithmetic follows the reference's evaluation order operation by operation;
  * build with -ffp-contract=off so that no multiply-add is fused.

@@ -1,20 +1,20 @@
 /*
  * pf_oracle.h -- CPU oracle for the Steinbach multi-phase-field time step.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: it is linked by the
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: it is linked by the
  * tests, by __graft_entry__.smoke() and by bench.py's cpu_baseline / reference
  * arm, never by the product library.  It is a plain-C FP64 restatement of the
  * reference's OpenMP CPU path (zhubq/PhaseField, C++-openmp-cuda/src/), with
  * the reference's operation order kept literally so that the product's FP64
  * GPU path can be compared bit-for-bit.
  *
- * Parity status: the phase-field sweep, the time-step driver and the thermo
- * evaluation are "parity unpinned" -- the reference ships no tests, golden
- * vectors or recorded outputs, and its C++ needs Blitz++ (an external library
- * absent here), so it cannot be built to produce any.  The partition and
- * diffusion sub-step are additionally checked against the reference's own
- * CUDA kernels (gpu_solver.cpp) compiled from source, where that build is
- * available.
+ * Parity status: the reference ships no tests, golden vectors or recorded
+ * outputs, and its C++ needs Blitz++ (absent here); its unmodified CPU sources
+ * are built against a minimal Blitz++ stand-in (oracle/blitz_shim), and full
+ * time steps of that build (phase sweep, driver, thermo, diffusion) are the
+ * golden vectors this oracle matches bit for bit (tests/test_golden.py).  The
+ * partition and diffusion sub-step are also checked against the reference's
+ * own CUDA kernels (gpu_solver.cpp) compiled from source.
  *
  * Layout (the reference's, phase_field.h:81-89): Blitz fortranArray with the
  * slot / phase index fastest, then x, y, z.  Here 0-based and flat:

@@ -5,9 +5,10 @@ also carries an independent restatement of the reference's positional
 configuration / thermodynamic readers (phase_field.cpp:166-330,
 thermo_functor.cpp:11-53) so the oracle never depends on the product's parser.
 
-Parity unpinned for the phase sweep (the reference has no tests or recorded
-outputs and cannot be built here); partition + diffusion are additionally
-checked against the reference's own CUDA kernels (see build_oracle.py).
+Pinned against the reference's own code: full time steps of its CPU path
+(built unmodified against the minimal Blitz++ stand-in, oracle/blitz_shim) and
+its CUDA partition + diffusion kernels, through the golden files of
+tests/golden (see build_oracle.py).
 """
 from __future__ import annotations
 

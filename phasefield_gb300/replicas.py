@@ -1,6 +1,6 @@
 """Host logic of multi-GPU runs: one process per GPU, no data-path collective.
 
-A single domain does not shard in this build (a slab decomposition would need a
+A single domain is not decomposed across GPUs (a slab decomposition would need a
 one-cell halo exchange per sweep), so N GPUs run independent replicas; the
 batched ensemble shards naturally -- its domains are independent -- so its
 domain list is split across the ranks.  Collectives are used only to time the

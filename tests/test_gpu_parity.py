@@ -5,7 +5,7 @@ Tolerances (stated per test):
 * FP64 plain path: bit-identical ids, and relative max-norm <= 1e-10 on every
   phase field, phase fraction and concentration (the kernels are built without
   multiply-add contraction, so in practice the difference is exactly 0).
-* FP32 compensated path: judged against the FP64 path on the same input.
+* FP32 compensated path: compared with the FP64 path on the same input.
 """
 import ctypes
 
