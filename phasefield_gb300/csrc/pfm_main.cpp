@@ -68,6 +68,11 @@ int main(int argc, char **argv) {
     pf_ctx *ctx = nullptr;
     check(pf_create(&m, prec, &ctx), "create context");
     check(pf_upload_state(ctx, ids.data(), phi.data(), phase.data(), conc.data(), C.data(), time), "upload");
+    if (m.coherent && spec.n_nuclei > 0) {  // the Fortran model's coherent partners, by its boundary-nucleation rule
+        std::vector<int32_t> partners(2 * (size_t)spec.n_nuclei);
+        check(pf_init_coherent(&m, &spec, partners.data()), "coherent partners");
+        check(pf_set_coherent_grains(ctx, partners.data(), spec.n_nuclei), "coherent partners");
+    }
     check(pf_use_graph(ctx, 0), "graph");
     int written = 0;
     check(pf_write_data(ctx, m.directory, 1, &written), "write data");

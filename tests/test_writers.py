@@ -70,3 +70,18 @@ def test_pfm_driver(gpu, tmp_path):
     assert r.returncode == 0, r.stderr
     assert "SIMULATION IS FINISHED" in r.stdout and "steps: 20" in r.stdout
     assert (out / "fraction_time.txt").exists()
+
+
+@pytest.mark.gpu
+def test_pfm_driver_fortran_options(gpu, tmp_path):
+    """The driver with the Fortran model's thermodynamics, solute drag and
+    coherent-grain mobility (it builds the coherent-partner table of its seeded
+    state): runs to completion on the FP64 path."""
+    W.write_thermo(str(tmp_path / "thermo_steel.txt"), "f90drag", coherent_npp0=0)
+    out = tmp_path / "out"
+    cfg = W.write_config(str(tmp_path / "c.txt"), grid=(48, 40, 1), directory=str(out), timestep_output=0.1,
+                         num_nuclei=3, num_grain=(4, 0, 0))
+    exe = os.path.join(os.path.dirname(pf.LIB_PATH), "..", "bin", "pfm")
+    r = subprocess.run([exe, cfg, "--steps", "10"], capture_output=True, text=True, cwd=str(tmp_path), timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "steps: 10" in r.stdout
