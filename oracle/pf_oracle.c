@@ -206,6 +206,12 @@ static double f90_dissipation(double Solution, double Driv, double Drag, double 
     return Solution;
 }
 
+/* DISSIPATION_ITERATION / _R as the sweep calls them, exported so the tests
+ * can check the velocity solve against a literal restatement of the Fortran. */
+double pfo_dissipation(double unchanged, double driv, double drag, double norm, int heating, const pfo_params *p) {
+    return f90_dissipation(unchanged, driv, drag, norm, heating, p);
+}
+
 /* The shared exp/log, exported so the tests can check them against the C
  * library and against the GPU build. */
 double pfo_exp(double x) { return pf_exp(x); }

@@ -125,6 +125,7 @@ void pfo_fractions(const pfo_model *m, const int32_t *ids, const double *phi, co
 int pfo_num_threads(void);
 /* Nonzero once a solute-drag iteration found no root (cleared by the caller). */
 extern int pfo_drag_failures;
+double pfo_dissipation(double unchanged, double driv, double drag, double norm, int heating, const pfo_params *p);
 double pfo_exp(double x);
 double pfo_log(double x);
 void pfo_set_num_threads(int n);

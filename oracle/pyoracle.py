@@ -341,7 +341,15 @@ def exp_log(x: np.ndarray):
     L.pfo_exp.restype = L.pfo_log.restype = ctypes.c_double
     L.pfo_exp.argtypes = L.pfo_log.argtypes = [ctypes.c_double]
     x = np.asarray(x, dtype=np.float64).ravel()
-    return (np.array([L.pfo_exp(float(v)) for v in x]), np.array([L.pfo_log(float(v)) if v > 0 else np.nan for v in x]))
+    return np.array([L.pfo_exp(float(v)) for v in x]), np.array([L.pfo_log(float(v)) for v in x])
+
+
+def dissipation(p: OParams, unchanged: float, driv: float, drag: float, norm: float, heating: int) -> float:
+    """The oracle's DISSIPATION_ITERATION (heating = 1) / _R (0) for one entry."""
+    L = lib()
+    L.pfo_dissipation.restype = ctypes.c_double
+    L.pfo_dissipation.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int, ctypes.POINTER(OParams)]
+    return L.pfo_dissipation(unchanged, driv, drag, norm, heating, ctypes.byref(p))
 
 
 def drag_failures(clear: bool = True) -> int:

@@ -443,3 +443,92 @@ def test_coherent_mobility_changes_the_oracle_step(tmp_path):
         runs.append(st)
     po.set_coherent(None)
     assert not np.array_equal(runs[0]["phi"], runs[1]["phi"])
+
+
+def _dissipation_literal(solution, driv, drag, norm, heating, p, T, exp, log):
+    """DISSIPATION_ITERATION (heating) / DISSIPATION_ITERATION_R (cooling),
+    sparse.f90:538-655, written out literally (with the drag pressure of
+    SOLUTE_DRAG_PB, sparse.f90:1005-1037); exp/log are passed in.  Returns
+    (solution, stopped): the _R form stops the Fortran program when no bracket
+    is found."""
+    f = np.float64  # IEEE arithmetic as in the C code (x / 0 is +-inf, not an exception)
+    drag0 = f(p.drag_drag0[0] if heating else p.drag_drag0[1])
+    de = f(p.drag_de_heat if heating else p.drag_de_cool)
+    corr = f(p.drag_corr[0] if heating else p.drag_corr[1])
+    ex0, u0, vmax = f(p.drag_ex0), f(p.drag_u0), f(p.drag_vmax)
+    driv, drag, norm = f(driv), f(drag), f(norm)
+
+    def sdpb(V0, E0, De, U0):
+        V = V0 / vmax
+        A = (De - E0) + V
+        B = (De + E0) + V
+        D0 = 1. - U0
+        Vu0 = V * U0
+        D1_d0 = (A - Vu0) / (A * D0 + (A - V) * U0 * exp(-(A - Vu0)))
+        D1 = D0 * D1_d0
+        U1 = 1. - D1
+        D2_d1 = (B - Vu0) / (B * D1 + (B * U1 - Vu0) * exp(-(B - Vu0)))
+        return (2. * De * U0 - ((A - V) / A * (Vu0 + log(D1_d0)) + (B - V) / B * (Vu0 + log(D2_d1)))) * 8.314 * T / 7.2e12
+
+    with np.errstate(all="ignore"):
+        return _dissipation_loops(solution, driv, drag, norm, heating, drag0, de, corr, ex0, u0, vmax, sdpb)
+
+
+def _dissipation_loops(solution, driv, drag, norm, heating, drag0, de, corr, ex0, u0, vmax, sdpb):
+    err2 = driv - drag * drag0
+    if err2 < 0.:
+        return 0., False
+    dv = 0.1 * vmax
+    v = np.float64(0.)
+    for _ in range(2):
+        for _ in range(40):
+            err1 = err2
+            v = v + dv
+            err2 = driv - v * norm - drag * (sdpb(v, ex0, de, u0) * corr)
+            if err1 * err2 <= 0.:
+                x1, x2 = v - dv, v
+                n = 0
+                while (x2 - x1) > 0.01 * x2:
+                    n += 1
+                    assert n < 10000
+                    tv = 0.5 * (x1 + x2)
+                    te = driv - tv * norm - drag * (sdpb(tv, ex0, de, u0) * corr)
+                    if err1 * te <= 0.:
+                        x2, err2 = tv, te
+                    else:
+                        x1, err1 = tv, te
+                return float(0.5 * (x1 + x2) * norm), False
+        v = driv / norm
+        dv = -0.2 * v
+        err2 = np.float64(-1.)
+    return solution, not heating
+
+
+@pytest.mark.parametrize("T", [1023.0, 1060.0])
+def test_drag_velocity_solve_oracle_equals_fortran_literal(tmp_path, T):
+    """The oracle's velocity solve equals the literal Fortran bit for bit (same
+    exp/log) over rates, drag weights and interface norms spanning the
+    no-drag, bracketed and no-bracket cases of both branches; a cooling solve
+    without a bracket is flagged where the Fortran stops."""
+    _, om = _drag_case(tmp_path, T=T)
+    p = po.params_at(om, 0.0)
+    exp = lambda x: np.float64(po.exp_log(np.array([x]))[0][0])
+    log = lambda x: np.float64(po.exp_log(np.array([x]))[1][0])
+    rng = np.random.default_rng(11)
+    seen = {"zero": 0, "root": 0, "none": 0}
+    # drag weights m_ij f3 sqrt(phi_i phi_j) and rates of the sweep's magnitudes
+    for t in range(320):
+        driv = float(10.0 ** rng.uniform(-1, 3.5))
+        drag = float(10.0 ** rng.uniform(10, 13))
+        # norm = f3 sqrt(phi (1 - phi)) is 0 for phi = 1: the second pass then
+        # starts at an infinite velocity and finds no bracket
+        norm = float(rng.uniform(0.05, 1.0)) if t < 300 else 0.0
+        heating = int(rng.integers(0, 2)) if t < 300 else t % 2
+        po.drag_failures()
+        got = po.dissipation(p, driv, driv, drag, norm, heating)
+        failed = po.drag_failures()
+        want, stopped = _dissipation_literal(driv, driv, drag, norm, heating, p, T, exp, log)
+        assert got == want, (driv, drag, norm, heating, got, want)
+        assert bool(failed) == stopped
+        seen["zero" if want == 0. else ("none" if want == driv or stopped else "root")] += 1
+    assert min(seen.values()) > 0, seen
