@@ -210,11 +210,11 @@ __device__ __forceinline__ R cpart(const AP<R> &P, const R *DS, int p, long long
 // Phase sweep; also writes the step's diffusion planes (step_planes) of the
 // new phase fractions.
 template <typename R>
-__global__ void k_fwd_phase(const AP<R> P, bool patch, const ushort4 *gid, const R *phi, const R *ph, const R *C,
+__global__ void k_fwd_phase(const AP<R> P, int patch, const ushort4 *gid, const R *phi, const R *ph, const R *C,
                             ushort4 *gid2, R *phi2, R *ph2, R *DS) {
     int ci, cj, ck;
     long long n;
-    if (!pf_cell_map(patch, P.ix, P.iy, ci, cj, ck, n)) return;
+    if (!pf_cell_map(patch, P.ix, P.iy, P.iz, ci, cj, ck, n)) return;
     Lst<R> L;
     build_list(P, ci, cj, ck, n, gid, phi, C, L);
     if (L.bulk) {
@@ -502,12 +502,12 @@ __global__ void k_seed(const AP<R> P, int obj, const R *ph, const R *C, double W
 // lam_C += driving-force part, the published neighbour-sum adjoints (ids, lS),
 // grad[0..1] += dJ/ds_m, dJ/ds_sigma.
 template <typename R>
-__global__ void k_bwd_phase_own(const AP<R> P, bool patch, const ushort4 *gid, const R *phi, const R *ph_pre,
+__global__ void k_bwd_phase_own(const AP<R> P, int patch, const ushort4 *gid, const R *phi, const R *ph_pre,
                                 const R *C, const R *lphi_post, const R *lph_post, R *lC, R *lphi_pre, R *lph_pre,
                                 int *pub_id, R *pub_l, double *grad) {
     int ci, cj, ck;
     long long n;
-    const bool in = pf_cell_map(patch, P.ix, P.iy, ci, cj, ck, n);
+    const bool in = pf_cell_map(patch, P.ix, P.iy, P.iz, ci, cj, ck, n);
     R gm = 0, gs = 0;  // s_m dJ/ds_m and s_sigma dJ/ds_sigma of this cell
     if (in) {
         Lst<R> L;
@@ -822,7 +822,7 @@ struct AdjCtx : pf_adj_impl {
         const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
         R *DS = Drec ? Drec : dscr;
         R *Csub = Drec ? Drec + 9 * N : nullptr;
-        const bool pt = pf_use_patch(P.iy);  // warps on 8 x 4 cell patches
+        const int pt = pf_use_patch(P.iy, P.iz);  // warps on compact cell patches
         k_fwd_phase<R><<<pf_map_grid(pt, P.ix, P.iy, P.iz), PF_CELL_THREADS, 0, s>>>(P, pt, g, phi, ph, C, g2, phi2,
                                                                                    ph2, DS);
         // Sub-step k writes buf[(n_sub-1-k) % 2] with buf = {C2, w_C2}: the last
@@ -1214,7 +1214,7 @@ static int adj_gradient_record(AdjCtx<R> *c, int obj, double grad[4]) {
     const size_t N = (size_t)c->N;
     AP<R> P = c->P;
     const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
-    const bool pt = pf_use_patch(P.iy);  // reverse phase sweep: warps on 8 x 4 cell patches
+    const int pt = pf_use_patch(P.iy, P.iz);  // reverse phase sweep: warps on compact cell patches
     const dim3 gp = pf_map_grid(pt, P.ix, P.iy, P.iz);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
@@ -1284,7 +1284,7 @@ static int adj_gradient(AdjCtx<R> *c, int obj, double grad[4]) {
     const unsigned nb = blocks(c->N);
     AP<R> P = c->P;
     const dim3 g3 = pf_cell_grid(P.ix, P.iy, P.iz);
-    const bool pt = pf_use_patch(P.iy);  // reverse phase sweep: warps on 8 x 4 cell patches
+    const int pt = pf_use_patch(P.iy, P.iz);  // reverse phase sweep: warps on compact cell patches
     const dim3 gp = pf_map_grid(pt, P.ix, P.iy, P.iz);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);

@@ -45,18 +45,27 @@ __device__ __forceinline__ bool pf_cell(int ix, int iy, int &i, int &j, int &k, 
 // The same cells with each warp on an 8 x 4 patch of a 32 x 8 block (grids
 // of at least 8 rows): kernels whose lanes branch on bulk versus interface
 // cells find a compact patch more often uniform than a 32-cell row.
-inline bool pf_use_patch(int iy) { return iy >= 8; }
-inline dim3 pf_map_grid(bool patch, int ix, int iy, int iz) {
+// 3D grids (iz > 1, map 2): 8 x 2 x 2 patches of 32 x 4 x 2 blocks instead.
+inline int pf_use_patch(int iy, int iz = 1) { return iy < 8 ? 0 : (iz > 1 ? 2 : 1); }
+inline dim3 pf_map_grid(int patch, int ix, int iy, int iz) {
+    if (patch == 2) return dim3((unsigned)((ix + 31) / 32), (unsigned)((iy + 3) / 4), (unsigned)((iz + 1) / 2));
     return patch ? dim3((unsigned)((ix + 31) / 32), (unsigned)((iy + 7) / 8), (unsigned)iz) : pf_cell_grid(ix, iy, iz);
 }
-__device__ __forceinline__ bool pf_cell_map(bool patch, int ix, int iy, int &i, int &j, int &k, long long &n) {
+__device__ __forceinline__ bool pf_cell_map(int patch, int ix, int iy, int iz, int &i, int &j, int &k,
+                                            long long &n) {
     if (!patch) return pf_cell(ix, iy, i, j, k, n);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    i = blockIdx.x * 32 + (w & 3) * 8 + (lane & 7);
-    j = blockIdx.y * 8 + (w >> 2) * 4 + (lane >> 3);
-    k = blockIdx.z;
+    if (patch == 2) {
+        i = blockIdx.x * 32 + (w & 3) * 8 + (lane & 7);
+        j = blockIdx.y * 4 + (w >> 2) * 2 + ((lane >> 3) & 1);
+        k = blockIdx.z * 2 + (lane >> 4);
+    } else {
+        i = blockIdx.x * 32 + (w & 3) * 8 + (lane & 7);
+        j = blockIdx.y * 8 + (w >> 2) * 4 + (lane >> 3);
+        k = blockIdx.z;
+    }
     n = i + (long long)ix * (j + (long long)iy * k);
-    return i < ix && j < iy;
+    return i < ix && j < iy && k < iz;
 }
 
 // Neighbours of (i,j,k) in the reference order x-, x+, y-, y+, z-, z+

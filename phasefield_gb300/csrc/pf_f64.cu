@@ -165,7 +165,7 @@ __device__ __forceinline__ bool pf_coh_has(const int *coh, int n_coh, int aus, i
 // EXT: compiled with the solute drag and the coherent mobility (the plain
 // model's instance carries neither, and keeps its register budget).
 template <bool EXT>
-__global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P, bool patch,
+__global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_step_params P, int patch,
                                                    const int *__restrict__ ids1,
                                                    const double *__restrict__ phi1,
                                                    int *__restrict__ ids2, double *__restrict__ phi2,
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) k_phase_f64(const __grid_constant__ pf_st
                                                    const int *__restrict__ coh, int n_coh) {
     int ci, cj, ck;
     long long n;
-    if (!pf_cell_map(patch, P.ix, P.iy, ci, cj, ck, n)) return;
+    if (!pf_cell_map(patch, P.ix, P.iy, P.iz, ci, cj, ck, n)) return;
     long long nbr[6];
     pf_neighbours3(ci, cj, ck, n, P.ix, P.iy, P.iz, nbr);
     const double cutoff = P.cutoff;
@@ -575,7 +575,7 @@ cudaError_t pf_launch_phase_f64(const pf_step_params &P, const int *ids1, const 
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const bool pt = pf_use_patch(P.iy);  // warps on 8 x 4 cell patches
+    const int pt = pf_use_patch(P.iy, P.iz);  // warps on compact cell patches
     const dim3 gp = pf_map_grid(pt, P.ix, P.iy, P.iz);
     if (P.drag_model || coherent)
         k_phase_f64<true><<<gp, PF_CELL_THREADS, 0, s>>>(P, pt, ids1, phi1, ids2, phi2, phase, conc1, C,
