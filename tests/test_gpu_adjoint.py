@@ -126,3 +126,17 @@ def test_fp32_gradient_tracks_fp64(gpu, tmp_path):
     b = g32.gradient(0)
     print(f"fp64 {a[:3]} fp32 {b[:3]}")
     np.testing.assert_allclose(b[:3], a[:3], rtol=2e-2, atol=1e-3 * np.max(np.abs(a[:3])))
+
+
+@pytest.mark.parametrize("K", [4, 0])
+def test_adjoint_3d_matches_central_differences(gpu, tmp_path, K):
+    """A 3D box (the phase kernels' 3D cell patches), checkpointed and record
+    mode, against central differences of the FP64 forward."""
+    steps = 10
+    A = _setup(tmp_path, K=K, grid=(16, 16, 8))
+    A.forward(steps)
+    g = A.gradient(0)
+    fd = [_fd(A, steps, 0, i) for i in range(3)]
+    for i in range(3):
+        scale = max(abs(fd[i]), 1e-3 * max(abs(x) for x in fd))
+        assert abs(g[i] - fd[i]) <= 2e-3 * scale, (i, g[i], fd[i])
